@@ -1,0 +1,298 @@
+#!/usr/bin/env python3
+"""Benchmark: GCUPS of the GB300 wavefront DP on one GPU (replicas across GPUs).
+
+Default workload: edit distance, one pair of 65536 x 65536 (4.3e9 cells), second
+sequence derived from the first by 10% seeded edits, plain path (one persistent
+kernel per alignment), int32 scores, score-only with O(n) boundary memory.
+
+Prints ONE JSON line (rank 0).  `value` is device-timed throughput with inputs
+resident in HBM; `e2e` is the same metric through the C ABI with host buffers
+(host->device copies and the device->host result read inside the timed region).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gme|reference]
+                  [--workload ed65536|lcs8192|sw32768|lcs32768]
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+# algorithmic integer operations per cell of the reference recurrences as written
+# (LCS.cpp:59-63: compare, select, add, max; ED.cpp:63-65: 3 adds, 2 mins, compare,
+# select; SW.cpp:45-47,63-65: 2 subtracts, compare+select, add, 3 maxes)
+OPS_PER_CELL = {0: 4, 1: 7, 2: 8}
+KIND_NAME = {0: "LCS", 1: "ED", 2: "SW"}
+INT_LANES_PER_SM = 128
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload(name: str):
+    from gpumemefficient_gb300 import synth
+    if name == "ed65536":
+        a, b = synth.ed_pair(65536)
+        return 1, a, b, {"workload": "edit distance, one pair 65536x65536, 10% seeded edits, plain path",
+                         "n1": 65536, "n2": 65536, "alphabet": 4, "edit_rate": 0.1,
+                         "seed": synth.SEED_ED, "ed_boundary": "ED.cpp (REF_CPU)"}
+    if name == "lcs8192":
+        a, b = synth.lcs_pair(8192)
+        return 0, a, b, {"workload": "LCS, one pair 8192x8192, plain path", "n1": 8192, "n2": 8192,
+                         "alphabet": 4, "seed": synth.SEED_LCS}
+    if name == "lcs32768":
+        a, b = synth.lcs_pair(32768)
+        return 0, a, b, {"workload": "LCS, one pair 32768x32768, plain path", "n1": 32768,
+                         "n2": 32768, "alphabet": 4, "seed": synth.SEED_LCS}
+    if name == "sw32768":
+        a, b = synth.sw_pair(32768)
+        return 2, a, b, {"workload": "Smith-Waterman, one pair 32768x32768, planted 2048 segment "
+                                     "mutated 15%, max score and cell", "n1": 32768, "n2": 32768,
+                         "alphabet": 20, "seed": synth.SEED_SW}
+    raise SystemExit(f"unknown workload {name}")
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int, interval_ms: int = 50):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                       f"-lms", str(interval_ms), "-i", str(device)],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for r in csv.reader(fh):
+                if len(r) >= 9:
+                    rows.append([x.strip() for x in r])
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((float(r[3]) for r in rows if r[3].replace(".", "").isdigit()), default=None)}
+
+
+def cpu_baseline(kind: int, a, b, target_s: float = 2.0, max_rows: int = None):
+    """The oracle port on all host threads over a bounded sample: the full first
+    sequence against a prefix of the second, grown until the run takes target_s."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    rows = 1024
+    limit = max_rows or len(b)
+    while True:
+        t0 = time.perf_counter()
+        O.align(kind, a, b[:rows], threads=threads, band_rows=64, chunk_cols=2048)
+        dt = time.perf_counter() - t0
+        if dt >= target_s or rows >= limit:
+            break
+        rows = min(limit, rows * 2 if dt < target_s / 4 else int(rows * target_s / dt) + 1)
+    cells = len(a) * rows
+    return {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": "port",
+            "sample": f"{KIND_NAME[kind]} {len(a)} columns x {rows} rows ({cells:.3g} cells), "
+                      f"oracle/oracle.c blocked wavefront on {threads} threads, {dt:.2f} s"}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    """Reference arm: the reference's CPU recurrence (oracle port; the reference sources are
+    not on this host) on all host threads, same metric and workload, bounded samples."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    kind, a, b, cfg = workload(args.workload)
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    rows = min(len(b), 4096 if len(a) >= 32768 else len(b))
+    for _ in range(args.warmup):
+        O.align(kind, a, b[:rows], threads=threads, band_rows=64, chunk_cols=2048)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.align(kind, a, b[:rows], threads=threads, band_rows=64, chunk_cols=2048)
+        times.append(time.perf_counter() - t0)
+    cells = len(a) * rows
+    tot = sum(times)
+    val = cells * len(times) / tot / 1e9
+    line = {"impl": "reference", "metric": "GCUPS on 1 GB300 (bit-exact)", "value": val, "unit": "GCUPS",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * tot / len(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded)", "config": cfg,
+            "cpu_baseline": {"value": val, "unit": "GCUPS", "cores": threads, "kind": "port",
+                             "sample": f"{KIND_NAME[kind]} {len(a)} columns x {rows} rows per step "
+                                       f"({cells:.3g} cells), oracle/oracle.c on {threads} threads"},
+            "e2e": {"value": val, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gme(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    import __graft_entry__ as ge
+    ge.build()
+    import gpumemefficient_gb300 as g
+    from oracle import oracle as O
+
+    kind, a, b, cfg = workload(args.workload)
+    n1, n2 = len(a), len(b)
+    cells = n1 * n2
+    ctx = g.Context(local)
+    stream = torch.cuda.Stream(device=local)
+    sc = g.scoring()
+    with torch.cuda.stream(stream):
+        d_a = torch.from_numpy(a).to(f"cuda:{local}")
+        d_b = torch.from_numpy(b).to(f"cuda:{local}")
+        d_out = torch.zeros(32, dtype=torch.uint8, device=f"cuda:{local}")
+        flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+    sp = stream.cuda_stream
+
+    def step():
+        ctx.align_device(kind, d_a.data_ptr(), n1, d_b.data_ptr(), n2, d_out.data_ptr(), sc=sc,
+                         stream=sp)
+
+    # parity of this exact workload with the oracle (outside the timed region)
+    step()
+    stream.synchronize()
+    res = g.Result.from_buffer_copy(bytes(d_out.cpu().numpy()))
+    o = O.align(kind, a, b, threads=os.cpu_count() or 1, band_rows=64, chunk_cols=2048)
+    parity = (res.status == 0 and res.score == o["score"] and
+              (kind != 2 or (res.sw_max, res.sw_max_y, res.sw_max_x) == (o["sw_max"], o["sw_y"], o["sw_x"])))
+
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+
+    clocks = ClockSampler(local)
+    time.sleep(0.15)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches0 = ctx.launches
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()            # L2 flush between timed steps (outside the events)
+            starts[i].record(stream)
+            step()
+            ends[i].record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launches - launches0
+    clk = clocks.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    t_dev = sum(step_ms) / 1e3
+    if ws > 1:
+        t = torch.tensor([t_dev], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(t.item())
+    value = ws * cells * args.steps / t_dev / 1e9
+
+    # end to end through the C ABI with pinned host buffers
+    ha = torch.from_numpy(a).pin_memory().numpy()
+    hb = torch.from_numpy(b).pin_memory().numpy()
+    e2e_steps = max(3, min(args.steps, 50))
+    for _ in range(2):
+        ctx.align(kind, ha, hb, sc=sc)
+    if ws > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        r = ctx.align(kind, ha, hb, sc=sc)
+    t_e2e = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([t_e2e], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = {"value": ws * cells * e2e_steps / t_e2e / 1e9, "unit": "GCUPS",
+           "h2d_bytes_per_step": int(a.nbytes + b.nbytes), "d2h_bytes_per_step": 32,
+           "steps": e2e_steps, "score_ok": r.score == o["score"]}
+
+    # roofline: integer ALU (the recurrence is min/max/add/select on int32)
+    props = torch.cuda.get_device_properties(local)
+    sms = props.multi_processor_count
+    mhz = clk.get("sm_mhz") or 1920.0
+    peak_tops = sms * INT_LANES_PER_SM * mhz * 1e6 / 1e12
+    mean_s = t_dev / args.steps
+    achieved = cells * OPS_PER_CELL[kind] / mean_s / 1e12
+    roof = {"bound": "int_alu", "achieved": achieved, "peak": peak_tops, "unit": "Tops/s",
+            "frac": achieved / peak_tops, "traffic": None,
+            "peak_basis": f"{sms} SMs x {INT_LANES_PER_SM} INT32 lanes x median SM clock "
+                          f"{mhz:.0f} MHz under load ({'measured' if clk.get('sm_mhz') else 'assumed'})",
+            "ops_per_cell": OPS_PER_CELL[kind], "kernel": "plain_kernel (whole step timed)"}
+
+    cpu = cpu_baseline(kind, a, b) if (rank == 0 and not args.no_cpu) else None
+    cfg = dict(cfg)
+    cfg.update({"l2": "flushed between timed steps (256 MiB write)", "plain_config": ctx.plain_config(n1, n2),
+                "parity_vs_oracle": "ok" if parity else "MISMATCH", "score": int(res.score)})
+    line = {"metric": "GCUPS on 1 GB300 (bit-exact)", "value": value, "unit": "GCUPS", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * mean_s,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded)", "config": cfg, "clocks": clk, "e2e": e2e,
+            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
+            "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gme", choices=["gme", "reference"])
+    p.add_argument("--workload", default="ed65536")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = p.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gme(args)
+
+
+if __name__ == "__main__":
+    main()

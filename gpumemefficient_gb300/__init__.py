@@ -1,0 +1,237 @@
+"""GB300 wavefront alignment DP (LCS / edit distance / Smith-Waterman).
+
+Python host side of ``libgme.so`` (the C ABI in ``include/gme.h``).  It mirrors
+the reference's host functions -- ``LCS``, ``ED`` and ``SW`` taking two integer
+sequences and returning the bottom-right cell (LCS/GPU_Hyperlane_Share.h:5,
+EditDistance/GPU_Hyperlane_Share.h:5, SmithWaterman/GPU_Hyperlane_Share.h:5) --
+and adds the richer calls of the C ABI (last row/column, SW maximum and its
+cell, device-pointer entry points, batched and served forms).
+
+There is no CPU fallback: importing this package without the built library
+raises, and every call runs on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+LCS_KIND, ED_KIND, SW_KIND = 0, 1, 2
+ED_REF_CPU, ED_STANDARD = 0, 1
+KINDS = {"lcs": LCS_KIND, "ed": ED_KIND, "sw": SW_KIND}
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libgme.so")
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory",
+          4: "device wait timed out", 5: "sizes could overflow int32 scores",
+          6: "request exceeds the HBM budget", 7: "not ready", 8: "server closed"}
+
+
+class GmeError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}" + (f": {msg}" if msg else ""))
+
+
+class Scoring(ctypes.Structure):
+    _fields_ = [("match", ctypes.c_int32), ("mismatch", ctypes.c_int32),
+                ("gap", ctypes.c_int32), ("ed_boundary", ctypes.c_int32)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("score", ctypes.c_int32), ("sw_max", ctypes.c_int32),
+                ("sw_max_y", ctypes.c_int64), ("sw_max_x", ctypes.c_int64),
+                ("status", ctypes.c_int32), ("kind", ctypes.c_int32)]
+
+
+class PlainConfig(ctypes.Structure):
+    _fields_ = [("rows_per_lane", ctypes.c_int32), ("warps_per_band", ctypes.c_int32),
+                ("grid", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_vp = ctypes.c_void_p
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def _declare(L):
+    c = ctypes
+    L.gme_create.argtypes = [c.c_int, c.POINTER(c.c_void_p)]
+    L.gme_destroy.argtypes = [_vp]
+    L.gme_last_error.argtypes = [_vp]
+    L.gme_last_error.restype = c.c_char_p
+    L.gme_status_string.restype = c.c_char_p
+    L.gme_default_scoring.restype = Scoring
+    L.gme_set_wait_timeout_ns.argtypes = [_vp, c.c_uint64]
+    L.gme_set_plain_config.argtypes = [_vp, c.POINTER(PlainConfig)]
+    L.gme_get_plain_config.argtypes = [_vp, c.c_int64, c.c_int64, c.POINTER(PlainConfig)]
+    L.gme_align.argtypes = [_vp, c.c_int, _vp, c.c_int64, _vp, c.c_int64, c.POINTER(Scoring),
+                            c.POINTER(Result), _vp, _vp]
+    L.gme_align_device.argtypes = [_vp, c.c_int, _vp, c.c_int64, _vp, c.c_int64,
+                                   c.POINTER(Scoring), _vp, _vp, _vp, _vp]
+    L.gme_debug_wait_timeout.argtypes = [_vp, c.c_uint64, c.POINTER(c.c_int32)]
+    L.gme_launch_count.argtypes = [_vp]
+    L.gme_launch_count.restype = c.c_int64
+    for name in ("gme_ref_lcs", "gme_ref_ed", "gme_ref_sw"):
+        f = getattr(L, name)
+        f.argtypes = [c.c_int32, c.c_int32, _vp, _vp]
+        f.restype = c.c_int32
+    return L
+
+
+def lib():
+    """The loaded libgme.so (raises if it has not been built)."""
+    global _lib
+    with _lib_lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise ImportError(f"libgme.so not built ({LIB_PATH}); run __graft_entry__.build()")
+            _lib = _declare(ctypes.CDLL(LIB_PATH))
+    return _lib
+
+
+def _check(status: int, ctx=None):
+    if status != 0:
+        msg = lib().gme_last_error(ctx).decode() if ctx else ""
+        raise GmeError(status, msg)
+
+
+def scoring(match: int = 3, mismatch: int = -3, gap: int = -2,
+            ed_boundary: int = ED_REF_CPU) -> Scoring:
+    """Scoring constants; the defaults are SmithWaterman/SW.cpp:45-47,63-65 and ED.cpp's border."""
+    return Scoring(match, mismatch, gap, ed_boundary)
+
+
+@dataclass
+class AlignResult:
+    score: int
+    sw_max: int = 0
+    sw_max_y: int = 0
+    sw_max_x: int = 0
+    last_row: Optional[np.ndarray] = None
+    last_col: Optional[np.ndarray] = None
+
+
+class Context:
+    """A device, its stream and a reusable workspace (one host thread at a time)."""
+
+    def __init__(self, device: int = 0):
+        h = ctypes.c_void_p()
+        _check(lib().gme_create(device, ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().gme_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def launches(self) -> int:
+        return int(lib().gme_launch_count(self.handle))
+
+    def set_timeout_ns(self, ns: int):
+        _check(lib().gme_set_wait_timeout_ns(self.handle, ns), self.handle)
+
+    def set_plain_config(self, rows_per_lane: int = 0, warps_per_band: int = 0, grid: int = 0):
+        cfg = PlainConfig(rows_per_lane, warps_per_band, grid, 0)
+        _check(lib().gme_set_plain_config(self.handle, ctypes.byref(cfg)), self.handle)
+
+    def plain_config(self, n1: int, n2: int) -> dict:
+        cfg = PlainConfig()
+        _check(lib().gme_get_plain_config(self.handle, n1, n2, ctypes.byref(cfg)), self.handle)
+        return {"rows_per_lane": cfg.rows_per_lane, "warps_per_band": cfg.warps_per_band,
+                "grid": cfg.grid}
+
+    def align(self, kind, a, b, sc: Optional[Scoring] = None, last_row: bool = False,
+              last_col: bool = False) -> AlignResult:
+        """One alignment from host arrays (the reference host functions' contract)."""
+        kind = KINDS.get(kind, kind) if isinstance(kind, str) else kind
+        a = np.ascontiguousarray(a, dtype=np.int32)
+        b = np.ascontiguousarray(b, dtype=np.int32)
+        sc = sc or scoring()
+        res = Result()
+        lr = np.empty(len(a) + 1, np.int32) if last_row else None
+        lc = np.empty(len(b) + 1, np.int32) if last_col else None
+        st = lib().gme_align(self.handle, kind, a.ctypes.data, len(a), b.ctypes.data, len(b),
+                             ctypes.byref(sc), ctypes.byref(res),
+                             lr.ctypes.data if lr is not None else None,
+                             lc.ctypes.data if lc is not None else None)
+        _check(st, self.handle)
+        return AlignResult(res.score, res.sw_max, res.sw_max_y, res.sw_max_x, lr, lc)
+
+    def align_device(self, kind, d_a: int, n1: int, d_b: int, n2: int, d_out: int,
+                     sc: Optional[Scoring] = None, d_last_row: int = 0, d_last_col: int = 0,
+                     stream: int = 0):
+        """Asynchronous alignment on device pointers; d_out points to a device gme_result."""
+        sc = sc or scoring()
+        _check(lib().gme_align_device(self.handle, kind, d_a, n1, d_b, n2, ctypes.byref(sc),
+                                      d_out, d_last_row or None, d_last_col or None,
+                                      stream or None), self.handle)
+
+    def debug_wait_timeout(self, timeout_ns: int) -> int:
+        """Runs a bounded device wait on a flag nothing sets; returns the kernel's status."""
+        ks = ctypes.c_int32(-1)
+        _check(lib().gme_debug_wait_timeout(self.handle, timeout_ns, ctypes.byref(ks)), self.handle)
+        return int(ks.value)
+
+
+_default_ctx: Optional[Context] = None
+_default_lock = threading.Lock()
+
+
+def default_context() -> Context:
+    global _default_ctx
+    with _default_lock:
+        if _default_ctx is None:
+            _default_ctx = Context(0)
+    return _default_ctx
+
+
+def align(kind, a, b, **kw) -> AlignResult:
+    sc_keys = {k: kw.pop(k) for k in ("match", "mismatch", "gap", "ed_boundary") if k in kw}
+    return default_context().align(kind, a, b, sc=scoring(**sc_keys) if sc_keys else None, **kw)
+
+
+# --- the reference's host functions (same names, argument meaning and result) ----------
+
+def _ref_call(kind, n1, n2, arr1, arr2):
+    a = np.ascontiguousarray(arr1, dtype=np.int32)[:n1]
+    b = np.ascontiguousarray(arr2, dtype=np.int32)[:n2]
+    if len(a) != n1 or len(b) != n2:
+        raise GmeError(1, "arrays shorter than n1/n2")
+    sc = scoring(ed_boundary=ED_STANDARD)  # the GPU reference's GPU_setInit border
+    return default_context().align(kind, a, b, sc=sc).score
+
+
+def LCS(n1, n2, arr1, arr2, paddX=3, paddY=1, table=None, tX=None, tY=None) -> int:
+    """LCS/GPU_Hyperlane_Share.h:5 -- length of the longest common subsequence."""
+    return _ref_call(LCS_KIND, n1, n2, arr1, arr2)
+
+
+def ED(n1, n2, arr1, arr2, paddX=3, paddY=1, table=None, tX=None, tY=None) -> int:
+    """EditDistance/GPU_Hyperlane_Share.h:5 -- edit distance (GPU_setInit border)."""
+    return _ref_call(ED_KIND, n1, n2, arr1, arr2)
+
+
+def SW(n1, n2, arr1, arr2, paddX=3, paddY=1, table=None, tX=None, tY=None) -> int:
+    """SmithWaterman/GPU_Hyperlane_Share.h:5 -- bottom-right cell of the SW table."""
+    return _ref_call(SW_KIND, n1, n2, arr1, arr2)

@@ -1,0 +1,352 @@
+// gme_api.cu -- the C ABI of include/gme.h: contexts, workspaces, the plain path.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "gme_common.cuh"
+#include "gme_internal.h"
+
+namespace gme {
+
+int Workspace::fail(cudaError_t e, const char *what) {
+  last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  return (e == cudaErrorMemoryAllocation) ? ST_NOMEM : ST_CUDA;
+}
+
+int Workspace::fail_msg(int status, const std::string &msg) {
+  last_error = msg;
+  return status;
+}
+
+static int grow(void **p, long long *cap, long long need, size_t elem, Workspace &ws, const char *what,
+                bool zero) {
+  if (*cap >= need && *p) return ST_OK;
+  if (ws.sync_stream) cudaStreamSynchronize(ws.sync_stream);
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  long long n = need + need / 4 + 1024;
+  cudaError_t e = cudaMalloc(p, (size_t)n * elem);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return ws.fail(e, what);
+  }
+  if (zero) {
+    e = cudaMemset(*p, 0, (size_t)n * elem);
+    if (e != cudaSuccess) return ws.fail(e, what);
+  }
+  *cap = n;
+  return ST_OK;
+}
+
+int Workspace::reserve(long long a_len, long long b_len, long long slot_words, int nbest) {
+  int rc;
+  if ((rc = grow((void **)&a_pad, &a_pad_cap, a_len, sizeof(int), *this, "cudaMalloc(a_pad)", false))) return rc;
+  if ((rc = grow((void **)&b_pad, &b_pad_cap, b_len, sizeof(int), *this, "cudaMalloc(b_pad)", false))) return rc;
+  if (slots_cap < slot_words || !slots) {
+    if ((rc = grow((void **)&slots, &slots_cap, slot_words, 8, *this, "cudaMalloc(slots)", true))) return rc;
+    slots_bytes = (size_t)slots_cap * 8;
+    tag_next = 1;  // fresh zeroed memory: every tag is unused
+  }
+  long long bc = best_cap;
+  if ((rc = grow(&best, &bc, nbest, 32, *this, "cudaMalloc(best)", false))) return rc;
+  best_cap = (int)bc;
+  if (!ctrl) {
+    cudaError_t e = cudaMalloc(&ctrl, 16 * sizeof(int));
+    if (e != cudaSuccess) return fail(e, "cudaMalloc(ctrl)");
+    cudaMemset(ctrl, 0, 16 * sizeof(int));
+  }
+  return ST_OK;
+}
+
+void Workspace::release() {
+  if (sync_stream) cudaStreamSynchronize(sync_stream);
+  cudaFree(a_pad); cudaFree(b_pad); cudaFree(slots); cudaFree(best); cudaFree(ctrl);
+  a_pad = b_pad = nullptr; slots = nullptr; best = nullptr; ctrl = nullptr;
+  a_pad_cap = b_pad_cap = slots_cap = 0; best_cap = 0;
+}
+
+// A kernel that waits, with the library's bounded wait, on a word nothing sets.
+__global__ void debug_wait_kernel(int *ctrl, const int *never, unsigned long long timeout_ns) {
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) abort_flag = 0;
+  __syncthreads();
+  Waiter W(timeout_ns, &ctrl[1], &abort_flag);
+  W.wait([&] { return ld_relaxed_gpu_s32(never) != 0; });
+}
+
+int debug_wait_timeout(Workspace &ws, unsigned long long timeout_ns, int *kernel_status,
+                       cudaStream_t st) {
+  int rc = ws.reserve(16, 16, 16, 1);
+  if (rc != ST_OK) return rc;
+  cudaError_t e = cudaMemsetAsync(ws.ctrl, 0, 16 * sizeof(int), st);
+  if (e != cudaSuccess) return ws.fail(e, "cudaMemsetAsync(ctrl)");
+  // ctrl[8] is never written by anyone: the wait can only end by its deadline
+  debug_wait_kernel<<<1, 32, 0, st>>>(ws.ctrl, ws.ctrl + 8, timeout_ns);
+  ws.launches += 1;
+  if ((e = cudaGetLastError()) != cudaSuccess) return ws.fail(e, "debug_wait_kernel");
+  int host[2] = {0, 0};
+  if ((e = cudaMemcpyAsync(host, ws.ctrl, 2 * sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return ws.fail(e, "cudaMemcpyAsync(ctrl)");
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return ws.fail(e, "cudaStreamSynchronize");
+  *kernel_status = host[1];
+  return ST_OK;
+}
+
+}  // namespace gme
+
+struct gme_context {
+  gme::Workspace ws;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  unsigned long long timeout_ns = 10ull * 1000 * 1000 * 1000;
+  gme_plain_config cfg{};
+  // device staging for the host-buffer entry points
+  int *d_a = nullptr; long long d_a_cap = 0;
+  int *d_b = nullptr; long long d_b_cap = 0;
+  int *d_row = nullptr; long long d_row_cap = 0;
+  int *d_col = nullptr; long long d_col_cap = 0;
+  gme_result *d_res = nullptr;
+  gme_result *h_res = nullptr;  // pinned
+};
+
+using gme::ST_OK;
+
+static gme_status to_status(int s) { return (gme_status)s; }
+
+static gme_status check_sizes(gme_context *ctx, gme_kind kind, int64_t n1, int64_t n2,
+                              const gme_scoring *sc) {
+  const int64_t LIM = (1ll << 30) - 4096;
+  if (kind < GME_LCS || kind > GME_SW) {
+    ctx->ws.last_error = "invalid kind";
+    return GME_ERR_INVALID;
+  }
+  if (n1 < 0 || n2 < 0) {
+    ctx->ws.last_error = "negative length";
+    return GME_ERR_INVALID;
+  }
+  if (n1 > LIM || n2 > LIM) {
+    ctx->ws.last_error = "sequence longer than 2^30-4096";
+    return GME_ERR_OVERFLOW;
+  }
+  if (kind == GME_SW) {
+    if (!sc) {
+      ctx->ws.last_error = "SW needs scoring constants";
+      return GME_ERR_INVALID;
+    }
+    long long m = std::max<long long>(std::max<long long>(llabs(sc->match), llabs(sc->mismatch)),
+                                      llabs(sc->gap));
+    if (m * (long long)(n1 + n2 + 2) >= (1ll << 30)) {
+      ctx->ws.last_error = "SW scores could overflow int32";
+      return GME_ERR_OVERFLOW;
+    }
+  }
+  if (kind == GME_ED && sc && sc->ed_boundary != GME_ED_REF_CPU && sc->ed_boundary != GME_ED_STANDARD) {
+    ctx->ws.last_error = "invalid ed_boundary";
+    return GME_ERR_INVALID;
+  }
+  return GME_OK;
+}
+
+static gme::Scoring to_scoring(const gme_scoring *sc) {
+  gme::Scoring s;
+  gme_scoring d = gme_default_scoring();
+  if (!sc) sc = &d;
+  s.match = sc->match;
+  s.mismatch = sc->mismatch;
+  s.gap = sc->gap;
+  s.ed_rule = sc->ed_boundary;
+  return s;
+}
+
+static int grow_dev(void **p, long long *cap, long long need, size_t elem, gme_context *ctx) {
+  if (*cap >= need && *p) return ST_OK;
+  cudaStreamSynchronize(ctx->stream);
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  long long n = need + need / 4 + 256;
+  cudaError_t e = cudaMalloc(p, (size_t)n * elem);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return ctx->ws.fail(e, "cudaMalloc(staging)");
+  }
+  *cap = n;
+  return ST_OK;
+}
+
+extern "C" {
+
+const char *gme_status_string(gme_status s) {
+  switch (s) {
+    case GME_OK: return "ok";
+    case GME_ERR_INVALID: return "invalid argument";
+    case GME_ERR_CUDA: return "CUDA error";
+    case GME_ERR_NOMEM: return "out of memory";
+    case GME_ERR_TIMEOUT: return "device wait timed out";
+    case GME_ERR_OVERFLOW: return "sizes could overflow int32 scores";
+    case GME_ERR_BUDGET: return "request exceeds the HBM budget";
+    case GME_ERR_NOT_READY: return "not ready";
+    case GME_ERR_CLOSED: return "server closed";
+  }
+  return "unknown status";
+}
+
+gme_scoring gme_default_scoring(void) {
+  gme_scoring s;
+  s.match = 3;      // SmithWaterman/SW.cpp:45-47
+  s.mismatch = -3;
+  s.gap = -2;       // SmithWaterman/SW.cpp:63-64
+  s.ed_boundary = GME_ED_REF_CPU;
+  return s;
+}
+
+gme_status gme_create(int device, gme_context **out) {
+  if (!out) return GME_ERR_INVALID;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || device < 0 || device >= n) return e != cudaSuccess ? GME_ERR_CUDA : GME_ERR_INVALID;
+  if ((e = cudaSetDevice(device)) != cudaSuccess) return GME_ERR_CUDA;
+  gme_context *ctx = new (std::nothrow) gme_context();
+  if (!ctx) return GME_ERR_NOMEM;
+  ctx->device = device;
+  ctx->ws.device = device;
+  cudaDeviceGetAttribute(&ctx->ws.sms, cudaDevAttrMultiProcessorCount, device);
+  if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    delete ctx;
+    return GME_ERR_CUDA;
+  }
+  ctx->ws.sync_stream = ctx->stream;
+  if ((e = cudaMalloc(&ctx->d_res, sizeof(gme_result))) != cudaSuccess ||
+      (e = cudaMallocHost(&ctx->h_res, sizeof(gme_result))) != cudaSuccess) {
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GME_ERR_NOMEM;
+  }
+  *out = ctx;
+  return GME_OK;
+}
+
+gme_status gme_destroy(gme_context *ctx) {
+  if (!ctx) return GME_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->ws.release();
+  cudaFree(ctx->d_a); cudaFree(ctx->d_b); cudaFree(ctx->d_row); cudaFree(ctx->d_col);
+  cudaFree(ctx->d_res);
+  cudaFreeHost(ctx->h_res);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return GME_OK;
+}
+
+const char *gme_last_error(const gme_context *ctx) {
+  return ctx ? ctx->ws.last_error.c_str() : "no context";
+}
+
+gme_status gme_set_wait_timeout_ns(gme_context *ctx, uint64_t ns) {
+  if (!ctx || ns == 0) return GME_ERR_INVALID;
+  ctx->timeout_ns = ns;
+  return GME_OK;
+}
+
+gme_status gme_set_plain_config(gme_context *ctx, const gme_plain_config *cfg) {
+  if (!ctx) return GME_ERR_INVALID;
+  if (!cfg) { ctx->cfg = gme_plain_config{}; return GME_OK; }
+  if ((cfg->rows_per_lane || cfg->warps_per_band) &&
+      !gme::plain_config_valid(cfg->rows_per_lane, cfg->warps_per_band)) {
+    ctx->ws.last_error = "plain config: rows_per_lane must be 4 or 8, warps_per_band 1, 2, 4 or 8";
+    return GME_ERR_INVALID;
+  }
+  if (cfg->grid < 0) return GME_ERR_INVALID;
+  ctx->cfg = *cfg;
+  return GME_OK;
+}
+
+gme_status gme_get_plain_config(const gme_context *ctx, int64_t n1, int64_t n2, gme_plain_config *r) {
+  if (!ctx || !r) return GME_ERR_INVALID;
+  int R, NW, grid;
+  gme::plain_auto_config(ctx->ws.sms, n1, n2, &R, &NW, &grid);
+  if (ctx->cfg.rows_per_lane) { R = ctx->cfg.rows_per_lane; NW = ctx->cfg.warps_per_band; }
+  const long long H = (long long)NW * 32 * R;
+  const long long nb = n2 > 0 ? (n2 + H - 1) / H : 0;
+  grid = (int)std::min<long long>(nb, ctx->ws.sms);
+  if (ctx->cfg.grid) grid = (int)std::min<long long>(nb, ctx->cfg.grid);
+  r->rows_per_lane = R;
+  r->warps_per_band = NW;
+  r->grid = grid;
+  r->reserved = 0;
+  return GME_OK;
+}
+
+gme_status gme_align_device(gme_context *ctx, gme_kind kind, const int32_t *d_a, int64_t n1,
+                            const int32_t *d_b, int64_t n2, const gme_scoring *sc,
+                            gme_result *d_out, int32_t *d_last_row, int32_t *d_last_col,
+                            void *stream) {
+  if (!ctx || !d_out || (n1 > 0 && !d_a) || (n2 > 0 && !d_b)) return GME_ERR_INVALID;
+  gme_status s = check_sizes(ctx, kind, n1, n2, sc);
+  if (s != GME_OK) return s;
+  cudaSetDevice(ctx->device);
+  gme_plain_config c;
+  gme_get_plain_config(ctx, n1, n2, &c);
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  cudaStream_t prev = ctx->ws.sync_stream;
+  ctx->ws.sync_stream = st;
+  int rc = gme::plain_run(ctx->ws, (int)kind, d_a, n1, d_b, n2, to_scoring(sc), d_out, d_last_row,
+                          d_last_col, st, c.rows_per_lane, c.warps_per_band, c.grid, ctx->timeout_ns);
+  ctx->ws.sync_stream = prev;
+  return to_status(rc);
+}
+
+gme_status gme_align(gme_context *ctx, gme_kind kind, const int32_t *a, int64_t n1,
+                     const int32_t *b, int64_t n2, const gme_scoring *sc, gme_result *out,
+                     int32_t *last_row, int32_t *last_col) {
+  if (!ctx || !out || (n1 > 0 && !a) || (n2 > 0 && !b)) return GME_ERR_INVALID;
+  gme_status s = check_sizes(ctx, kind, n1, n2, sc);
+  if (s != GME_OK) return s;
+  cudaSetDevice(ctx->device);
+  int rc;
+  if ((rc = grow_dev((void **)&ctx->d_a, &ctx->d_a_cap, std::max<int64_t>(n1, 1), 4, ctx)) ||
+      (rc = grow_dev((void **)&ctx->d_b, &ctx->d_b_cap, std::max<int64_t>(n2, 1), 4, ctx)))
+    return to_status(rc);
+  if (last_row && (rc = grow_dev((void **)&ctx->d_row, &ctx->d_row_cap, n1 + 1, 4, ctx))) return to_status(rc);
+  if (last_col && (rc = grow_dev((void **)&ctx->d_col, &ctx->d_col_cap, n2 + 1, 4, ctx))) return to_status(rc);
+  cudaStream_t st = ctx->stream;
+  cudaError_t e;
+  if (n1 > 0 && (e = cudaMemcpyAsync(ctx->d_a, a, (size_t)n1 * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return to_status(ctx->ws.fail(e, "cudaMemcpyAsync(a)"));
+  if (n2 > 0 && (e = cudaMemcpyAsync(ctx->d_b, b, (size_t)n2 * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return to_status(ctx->ws.fail(e, "cudaMemcpyAsync(b)"));
+  s = gme_align_device(ctx, kind, ctx->d_a, n1, ctx->d_b, n2, sc, ctx->d_res,
+                       last_row ? ctx->d_row : nullptr, last_col ? ctx->d_col : nullptr, st);
+  if (s != GME_OK) return s;
+  if ((e = cudaMemcpyAsync(ctx->h_res, ctx->d_res, sizeof(gme_result), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return to_status(ctx->ws.fail(e, "cudaMemcpyAsync(result)"));
+  if (last_row && (e = cudaMemcpyAsync(last_row, ctx->d_row, (size_t)(n1 + 1) * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return to_status(ctx->ws.fail(e, "cudaMemcpyAsync(last_row)"));
+  if (last_col && (e = cudaMemcpyAsync(last_col, ctx->d_col, (size_t)(n2 + 1) * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return to_status(ctx->ws.fail(e, "cudaMemcpyAsync(last_col)"));
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return to_status(ctx->ws.fail(e, "cudaStreamSynchronize"));
+  *out = *ctx->h_res;
+  if (out->status != 0) {
+    ctx->ws.last_error = "device-side wait timed out";
+    return to_status(out->status);
+  }
+  return GME_OK;
+}
+
+gme_status gme_debug_wait_timeout(gme_context *ctx, uint64_t timeout_ns, int32_t *kernel_status) {
+  if (!ctx || !kernel_status || timeout_ns == 0 || timeout_ns > 60ull * 1000 * 1000 * 1000)
+    return GME_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  return to_status(gme::debug_wait_timeout(ctx->ws, timeout_ns, kernel_status, ctx->stream));
+}
+
+int64_t gme_launch_count(const gme_context *ctx) { return ctx ? ctx->ws.launches : -1; }
+
+}  // extern "C"

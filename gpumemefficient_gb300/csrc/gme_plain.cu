@@ -1,0 +1,597 @@
+// gme_plain.cu -- one alignment per call: a single persistent wavefront kernel.
+//
+// Replaces the reference's per-tile-row launch loop (EditDistance/
+// GPU_Hyperlane_Share.cu:752-764, one <<<1,1024>>> GPU() launch per tile row on
+// SM-count streams, rows chained by the dev_lock spin counters at :110-129) and
+// the full (n+pad)^2 int table it keeps in device memory (:698-713).
+//
+// Decomposition
+//   * The table's rows are cut into BANDS of H = NW*32*R rows (the reference's
+//     "tile row" / curBatch).  A band is owned by one CTA; CTAs claim bands in
+//     order from an atomic ticket, so the CTA that waits on band b-1 always
+//     waits on a CTA that is already running (no residency assumption).
+//   * Inside a band each compute warp owns 32*R rows and each lane R of them
+//     (a vertical strip).  At warp step s, lane t, row r computes column
+//     x = s - t*R - r: the whole warp sweeps one anti-diagonal per step, so the
+//     R cells of a lane are independent (instruction-level parallelism) and the
+//     only value crossing lanes each step is the bottom cell of the lane above,
+//     carried with one __shfl_sync (the LCS-SHFL idea, LCS-SHFL/
+//     GPU_Hyperlane_Share.cu:339-361).  Over a run of steps a warp's cells form a
+//     parallelogram: the reference's "hyperlane" tile (GPU_Hyperlane_Share.cu
+//     :320-496), here kept in registers instead of a skewed shared tile.
+//   * Warps of a band hand their bottom row to the next warp through a
+//     shared-memory ring with release/acquire progress counters (replacing
+//     moveToShare/moveToGlobal, :24-79).  Lane 31 feeds the incoming row to
+//     lane 0 through the same shuffle.
+//   * Bands hand their bottom row to the next band through a global buffer of
+//     64-bit words {tag, value}.  The tag names the producing band, so a
+//     consumer polls the data itself (one L2 round trip, no separate flag) and
+//     the reference's non-atomic dev_lock += 1 / unbounded volatile spin becomes
+//     a tagged, bounded wait.  One extra warp per CTA (the I/O warp) moves rows
+//     between global memory and the first/last rings.
+//   * Nothing of the table is kept: memory is O(n1) per band in flight, the
+//     last row/column are produced on the fly.
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+
+#include "gme_common.cuh"
+#include "gme_internal.h"
+
+namespace gme {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int RING = 512;   // columns per ring (power of two)
+constexpr int PADL = 261;   // left pad of the staged a[]: >= 32*8+5 and == 1 (mod 4)
+constexpr int PADR = 320;   // right pad (>= 32*8 + 16 + prefetch)
+
+struct SwBest {
+  int v;
+  int pad;
+  long long y, x;
+};
+
+__device__ __forceinline__ bool better(const SwBest &a, const SwBest &b) {
+  // larger value first; among equals the first cell in row-major order
+  if (a.v != b.v) return a.v > b.v;
+  if (a.y != b.y) return a.y < b.y;
+  return a.x < b.x;
+}
+
+struct PlainParams {
+  const int *a_pad;  // a_pad[PADL + i] = a[i]
+  const int *b_pad;  // b_pad[i] = b[i], length nbands*H
+  int N, M;          // n1 (columns, over a), n2 (rows, over b)
+  int H, nbands;
+  int nslot;
+  long long slot_stride;          // u64 words per slot
+  unsigned long long *slots;      // nslot * slot_stride tagged words
+  unsigned tag0;                  // tag of band b = tag0 + b
+  int *ctrl;                      // [0] ticket, [1] status
+  int *last_col;                  // optional, device, n2+1 values
+  SwBest *best;                   // one per CTA
+  Scoring sc;
+  unsigned long long timeout_ns;
+};
+
+template <int NW> struct __align__(16) PlainSmem {
+  int ring[NW + 1][RING];
+  int prod[NW + 1];
+  int cons[NW + 1];
+  int band;
+  int abort;
+  SwBest best[NW + 1];
+};
+
+__device__ __forceinline__ int4 ldg4(const int *p) { return __ldg(reinterpret_cast<const int4 *>(p)); }
+
+// ---------------------------------------------------------------------------
+// Four wavefront steps of one lane (R rows).  CHECKED: some cells of the warp
+// fall outside 1 <= x <= N (ramp-in/out) and hold their value.  PADROWS: rows
+// beyond n2 copy the row above, so the warp's bottom row equals row n2.
+// ---------------------------------------------------------------------------
+template <int KIND, int R, bool CHECKED, bool PADROWS>
+__device__ __forceinline__ void steps4(const Rec<KIND> &rec, int (&cur)[R], int (&prv)[R],
+                                       int &recv, int &recv_prev, const int (&win)[R + 4],
+                                       const int (&bs)[R], const int (&inv)[4], int (&outq)[4],
+                                       int s0, int lane, int N, unsigned padmask,
+                                       int (&smax)[R], int (&sstep)[R]) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int s = s0 + q;
+    const int send = (lane == 31) ? inv[q] : cur[R - 1];
+    outq[q] = cur[R - 1];  // lane 31: bottom cell after step s-1 (column s-32R)
+    recv_prev = recv;
+    recv = __shfl_sync(FULL, send, (lane + 31) & 31);
+    int nv[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int up = r ? cur[r - 1] : recv;
+      const int dg = r ? prv[r - 1] : recv_prev;
+      const int D = dg + (win[R + q - r] == bs[r] ? rec.ceq : rec.cne);
+      int v = rec.cell(up, cur[r], D);
+      if (CHECKED) {
+        const int x = s - lane * R - r;
+        if ((unsigned)(x - 1) >= (unsigned)N) v = cur[r];
+      }
+      if (PADROWS) {
+        if (padmask & (1u << r)) v = up;
+      }
+      if (KIND == K_SW) {
+        if (v > smax[r]) { smax[r] = v; sstep[r] = s; }
+      }
+      nv[r] = v;
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) { prv[r] = cur[r]; cur[r] = nv[r]; }
+  }
+}
+
+// One compute warp sweeping its 32*R rows of a band across all N columns.
+template <int KIND, int R, int NW>
+__device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, int warp, int lane,
+                             Waiter &W, SwBest &tb) {
+  const Rec<KIND> rec(P.sc);
+  const int N = P.N, M = P.M;
+  const int yl = band * P.H + warp * 32 * R + lane * R + 1;  // first row of this lane
+  int bs[R], cur[R], prv[R], smax[R], sstep[R];
+#pragma unroll
+  for (int r = 0; r < R; r += 4) {
+    int4 q = ldg4(P.b_pad + (yl - 1 + r));
+    bs[r] = q.x; bs[r + 1] = q.y; bs[r + 2] = q.z; bs[r + 3] = q.w;
+  }
+  unsigned padmask = 0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    cur[r] = Rec<KIND>::left(yl + r);
+    prv[r] = cur[r];
+    smax[r] = 0;
+    sstep[r] = 0;
+    if (yl + r > M) padmask |= 1u << r;
+  }
+  const bool padwarp = __any_sync(FULL, padmask != 0);
+
+  // Symbol window: win[k] = a_pad[base + 4j - R + k]; the symbol of row r at
+  // step 4j+q is win[R+q-r] (column x = 4j+q - lane*R - r, a[x-1]).
+  const long long base = PADL - 1 - lane * R;
+  int win[R + 4];
+#pragma unroll
+  for (int k = 0; k < R + 4; k += 4) {
+    int4 q = ldg4(P.a_pad + base - R + k);
+    win[k] = q.x; win[k + 1] = q.y; win[k + 2] = q.z; win[k + 3] = q.w;
+  }
+  int4 nextq = ldg4(P.a_pad + base + 4);
+
+  int recv = 0, recv_prev = 0;
+  int *ring_in = S.ring[warp];
+  int *ring_out = S.ring[warp + 1];
+  int *prod_in = &S.prod[warp], *cons_in = &S.cons[warp];
+  int *prod_out = &S.prod[warp + 1], *cons_out = &S.cons[warp + 1];
+  const int j_end = N / 4 + 8 * R;  // last chunk: lane 31's last row reaches column N
+
+  for (int j = 0; j <= j_end; ++j) {
+    const int s0 = 4 * j;
+    // incoming row (columns 4j..4j+3) for lane 0, read by lane 31
+    const int need = min(s0 + 4, N + 1);
+    if (!W.wait([&] { return ld_acquire_cta(prod_in) >= need; })) return;
+    int inv[4] = {0, 0, 0, 0};
+    if (lane == 31) {
+      int4 q = *reinterpret_cast<const int4 *>(&ring_in[s0 & (RING - 1)]);
+      inv[0] = q.x; inv[1] = q.y; inv[2] = q.z; inv[3] = q.w;
+    }
+    const int4 q_now = nextq;
+    nextq = ldg4(P.a_pad + base + 4 * (j + 2));
+
+    int outq[4];
+    const bool steady = (s0 >= 32 * R) && (s0 + 3 <= N);
+    if (padwarp) {
+      steps4<KIND, R, true, true>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0, lane, N,
+                                  padmask, smax, sstep);
+    } else if (steady) {
+      steps4<KIND, R, false, false>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0, lane, N,
+                                    padmask, smax, sstep);
+    } else {
+      steps4<KIND, R, true, false>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0, lane, N,
+                                   padmask, smax, sstep);
+    }
+    if (lane == 31) st_release_cta(cons_in, s0 + 4);
+
+    // outgoing row: columns 4jo..4jo+3, jo = j - 8R
+    const int jo = j - 8 * R;
+    if (jo >= 0) {
+      const int pos = 4 * jo;
+      if (!W.wait([&] { return ld_acquire_cta(cons_out) >= pos + 4 - RING; })) return;
+      if (lane == 31) {
+        *reinterpret_cast<int4 *>(&ring_out[pos & (RING - 1)]) = make_int4(outq[0], outq[1], outq[2], outq[3]);
+        st_release_cta(prod_out, pos + 4);
+      }
+    }
+    // slide the symbol window by four columns
+#pragma unroll
+    for (int k = 0; k < R; ++k) win[k] = win[k + 4];
+    win[R] = q_now.x; win[R + 1] = q_now.y; win[R + 2] = q_now.z; win[R + 3] = q_now.w;
+  }
+
+  // every row now holds its value at column N (cells beyond N were held)
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const long long y = yl + r;
+    if (y <= M) {
+      if (P.last_col) P.last_col[y] = Rec<KIND>::to_v(cur[r], N, y);
+      if (KIND == K_SW && smax[r] > 0) {
+        SwBest c = {smax[r], 0, y, (long long)(sstep[r] - lane * R - r)};
+        if (better(c, tb)) tb = c;
+      }
+    }
+  }
+}
+
+// The I/O warp of a band: incoming row (global -> ring 0) and outgoing row
+// (ring `active` -> global), each lane moving four consecutive columns.
+template <int KIND, int NW>
+__device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int active, int lane,
+                        Waiter &W) {
+  const int N1 = P.N + 1;
+  const unsigned long long *src =
+      band > 0 ? P.slots + (long long)((band - 1) % P.nslot) * P.slot_stride : nullptr;
+  unsigned long long *dst = P.slots + (long long)(band % P.nslot) * P.slot_stride;
+  const unsigned src_tag = P.tag0 + (unsigned)(band - 1);
+  const unsigned long long dst_tag = (unsigned long long)(P.tag0 + (unsigned)band) << 32;
+  int *ring0 = S.ring[0];
+  int *ringo = S.ring[active];
+  int in_pos = 0, out_pos = 0;
+  unsigned idle = 0;
+  unsigned long long deadline = 0;
+
+  while (in_pos < N1 || out_pos < N1) {
+    bool moved = false;
+    if (in_pos < N1) {
+      const int space = RING - (in_pos - ld_acquire_cta(&S.cons[0]));
+      const int want = min(N1 - in_pos, space);
+      if (want > 0) {
+        const int p = in_pos + 4 * lane;
+        int v[4] = {0, 0, 0, 0};
+        bool ok = true;
+        if (4 * lane < want) {
+          if (band == 0) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) v[k] = Rec<KIND>::top(p + k, P.sc.ed_rule);
+          } else {
+            const volatile unsigned long long *sp = src + p;
+            unsigned long long w0, w1, w2, w3;
+            asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2];" : "=l"(w0), "=l"(w1) : "l"(sp));
+            asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2+16];" : "=l"(w2), "=l"(w3) : "l"(sp));
+            const unsigned long long w[4] = {w0, w1, w2, w3};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              v[k] = (int)(unsigned)w[k];
+              if (p + k < N1 && (unsigned)(w[k] >> 32) != src_tag) ok = false;
+            }
+          }
+        } else {
+          ok = false;
+        }
+        const unsigned okm = __ballot_sync(FULL, ok);
+        const int lanes_ok = (okm == FULL) ? 32 : (__ffs(~okm) - 1);
+        const int n = min(4 * lanes_ok, want);
+        if (n > 0) {
+          if (4 * lane < n) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) ring0[(p + k) & (RING - 1)] = v[k];
+          }
+          __syncwarp();
+          if (lane == 0) st_release_cta(&S.prod[0], in_pos + n);
+          in_pos += n;
+          moved = true;
+        }
+      }
+    }
+    if (out_pos < N1) {
+      const int avail = min(ld_acquire_cta(&S.prod[active]), N1);
+      const int n = min(avail - out_pos, 128);
+      if (n > 0) {
+        const int p = out_pos + 4 * lane;
+        if (4 * lane < n) {
+          const int4 q = *reinterpret_cast<const int4 *>(&ringo[p & (RING - 1)]);
+          volatile unsigned long long *dp = dst + p;
+          const unsigned long long w0 = dst_tag | (unsigned)q.x, w1 = dst_tag | (unsigned)q.y;
+          const unsigned long long w2 = dst_tag | (unsigned)q.z, w3 = dst_tag | (unsigned)q.w;
+          asm volatile("st.volatile.global.v2.u64 [%0], {%1,%2};" :: "l"(dp), "l"(w0), "l"(w1) : "memory");
+          asm volatile("st.volatile.global.v2.u64 [%0+16], {%1,%2};" :: "l"(dp), "l"(w2), "l"(w3) : "memory");
+        }
+        __syncwarp();
+        if (lane == 0) st_release_cta(&S.cons[active], out_pos + n);
+        out_pos += n;
+        moved = true;
+      }
+    }
+    if (moved) {
+      idle = 0;
+    } else {
+      // bounded wait: nothing could move this round
+      if (idle == 0) deadline = globaltimer_ns() + P.timeout_ns;
+      if ((++idle & 63u) == 0) {
+        if (S.abort) return;
+        if (ld_relaxed_gpu_s32(&P.ctrl[1]) != 0) { S.abort = 1; return; }
+        if (globaltimer_ns() > deadline) {
+          atomicCAS(&P.ctrl[1], 0, ST_TIMEOUT);
+          S.abort = 1;
+          return;
+        }
+      }
+      __nanosleep(64);
+    }
+  }
+}
+
+template <int KIND, int R, int NW>
+__global__ void __launch_bounds__((NW + 1) * 32, 1) plain_kernel(PlainParams P) {
+  __shared__ PlainSmem<NW> S;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) S.abort = 0;
+  __syncthreads();
+  Waiter W(P.timeout_ns, &P.ctrl[1], &S.abort);
+  SwBest tb = {0, 0, 0, 0};
+  for (;;) {
+    if (threadIdx.x == 0) {
+      S.band = S.abort ? P.nbands : atomicAdd(&P.ctrl[0], 1);
+#pragma unroll
+      for (int k = 0; k <= NW; ++k) { S.prod[k] = 0; S.cons[k] = 0; }
+    }
+    __syncthreads();
+    const int band = S.band;
+    if (band >= P.nbands) break;
+    const int rows_left = P.M - band * P.H;
+    const int active = min(NW, (rows_left + 32 * R - 1) / (32 * R));
+    if (warp < NW) {
+      if (warp < active) compute_band<KIND, R, NW>(P, S, band, warp, lane, W, tb);
+    } else {
+      io_band<KIND, NW>(P, S, band, active, lane, W);
+    }
+    __syncthreads();
+  }
+  if (KIND == K_SW) {
+    // block reduction of the per-thread first maxima
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      SwBest c;
+      c.v = __shfl_down_sync(FULL, tb.v, o);
+      c.y = __shfl_down_sync(FULL, tb.y, o);
+      c.x = __shfl_down_sync(FULL, tb.x, o);
+      c.pad = 0;
+      if (better(c, tb)) tb = c;
+    }
+    if (lane == 0) S.best[warp] = tb;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      SwBest b = S.best[0];
+      for (int k = 1; k <= NW; ++k)
+        if (better(S.best[k], b)) b = S.best[k];
+      P.best[blockIdx.x] = b;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Staging, finishing and degenerate-size kernels.
+// ---------------------------------------------------------------------------
+__global__ void stage_kernel(const int *__restrict__ a, int N, const int *__restrict__ b, int M,
+                             int *__restrict__ a_pad, long long a_pad_len, int *__restrict__ b_pad,
+                             long long b_pad_len) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a_pad_len; i += stride) {
+    const long long k = i - PADL;
+    a_pad[i] = (k >= 0 && k < N) ? a[k] : 0;
+  }
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < b_pad_len; i += stride)
+    b_pad[i] = (i < M) ? b[i] : 0;
+}
+
+template <int KIND>
+__global__ void finish_row_kernel(const unsigned long long *__restrict__ last_slot, int N, int M,
+                                  int *__restrict__ last_row) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x <= N) last_row[x] = Rec<KIND>::to_v((int)(unsigned)last_slot[x], x, M);
+}
+
+template <int KIND>
+__global__ void finish_result_kernel(const unsigned long long *__restrict__ last_slot, int N, int M,
+                                     int rule, const SwBest *__restrict__ best, int nbest,
+                                     const int *ctrl, gme_result *out, int *last_col) {
+  __shared__ SwBest sb[32];
+  SwBest b = {0, 0, 0, 0};
+  if (KIND == K_SW) {
+    for (int i = threadIdx.x; i < nbest; i += blockDim.x)
+      if (better(best[i], b)) b = best[i];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    SwBest c;
+    c.v = __shfl_down_sync(FULL, b.v, o);
+    c.y = __shfl_down_sync(FULL, b.y, o);
+    c.x = __shfl_down_sync(FULL, b.x, o);
+    c.pad = 0;
+    if (better(c, b)) b = c;
+  }
+  if (lane == 0) sb[warp] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x / 32); ++k)
+      if (better(sb[k], b)) b = sb[k];
+    gme_result r;
+    r.score = Rec<KIND>::to_v((int)(unsigned)last_slot[N], N, M);
+    r.sw_max = KIND == K_SW ? b.v : 0;
+    r.sw_max_y = KIND == K_SW ? b.y : 0;
+    r.sw_max_x = KIND == K_SW ? b.x : 0;
+    r.status = ctrl[1];
+    r.kind = KIND;
+    *out = r;
+    if (last_col) last_col[0] = Rec<KIND>::to_v(Rec<KIND>::top(N, rule), N, 0);  // row 0, column n1
+  }
+}
+
+// n1 == 0 or n2 == 0: the table is its borders.
+template <int KIND>
+__global__ void degenerate_kernel(int N, int M, int rule, int *last_row, int *last_col, gme_result *out) {
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  // row n2 when n2 == 0 is row 0; otherwise (n1 == 0) it is the single value column-0 at n2
+  for (long long x = tid; x <= N && last_row; x += stride)
+    last_row[x] = (M == 0) ? Rec<KIND>::to_v(Rec<KIND>::top(x, rule), x, 0)
+                           : Rec<KIND>::to_v(Rec<KIND>::left(M), 0, M);
+  for (long long y = tid; y <= M && last_col; y += stride)
+    last_col[y] = (y == 0) ? Rec<KIND>::to_v(Rec<KIND>::top(N, rule), N, 0)
+                           : Rec<KIND>::to_v(Rec<KIND>::left(y), 0, y);
+  if (tid == 0) {
+    gme_result r;
+    r.score = (M == 0) ? Rec<KIND>::to_v(Rec<KIND>::top(N, rule), N, 0)
+                       : Rec<KIND>::to_v(Rec<KIND>::left(M), 0, M);
+    r.sw_max = 0; r.sw_max_y = 0; r.sw_max_x = 0; r.status = 0; r.kind = KIND;
+    *out = r;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+template <int KIND, int R, int NW>
+static cudaError_t launch_plain_t(const PlainParams &P, int grid, cudaStream_t st) {
+  plain_kernel<KIND, R, NW><<<grid, (NW + 1) * 32, 0, st>>>(P);
+  return cudaGetLastError();
+}
+
+template <int KIND>
+static cudaError_t launch_plain_k(int R, int NW, const PlainParams &P, int grid, cudaStream_t st) {
+  if (R == 4) {
+    switch (NW) {
+      case 1: return launch_plain_t<KIND, 4, 1>(P, grid, st);
+      case 2: return launch_plain_t<KIND, 4, 2>(P, grid, st);
+      case 4: return launch_plain_t<KIND, 4, 4>(P, grid, st);
+      case 8: return launch_plain_t<KIND, 4, 8>(P, grid, st);
+    }
+  } else if (R == 8) {
+    switch (NW) {
+      case 1: return launch_plain_t<KIND, 8, 1>(P, grid, st);
+      case 2: return launch_plain_t<KIND, 8, 2>(P, grid, st);
+      case 4: return launch_plain_t<KIND, 8, 4>(P, grid, st);
+      case 8: return launch_plain_t<KIND, 8, 8>(P, grid, st);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+bool plain_config_valid(int R, int NW) {
+  return (R == 4 || R == 8) && (NW == 1 || NW == 2 || NW == 4 || NW == 8);
+}
+
+// Automatic shape: enough bands to cover the SMs, as few band boundaries as
+// possible (each costs one L2 hand-off on the critical path).
+void plain_auto_config(int sms, long long n1, long long n2, int *R, int *NW, int *grid) {
+  (void)n1;
+  int r = 4, nw = 4;
+  const long long rows_per_sm = (n2 + sms - 1) / sms;
+  if (rows_per_sm >= 8 * 32 * 4) { r = 8; nw = 8; }
+  else if (rows_per_sm >= 4 * 32 * 4) { r = 4; nw = 4; }
+  else if (rows_per_sm >= 2 * 32 * 4) { r = 4; nw = 2; }
+  else { r = 4; nw = 1; }
+  *R = r;
+  *NW = nw;
+  const long long H = (long long)nw * 32 * r;
+  const long long nb = (n2 + H - 1) / H;
+  *grid = (int)std::min<long long>(nb, (long long)sms);
+}
+
+int plain_run(Workspace &ws, int kind, const int *d_a, long long n1, const int *d_b, long long n2,
+              const Scoring &sc, gme_result *d_out, int *d_last_row, int *d_last_col,
+              cudaStream_t st, int R, int NW, int grid, unsigned long long timeout_ns) {
+  const int N = (int)n1, M = (int)n2;
+  cudaError_t e;
+  if (N == 0 || M == 0) {
+    const int threads = 256;
+    const long long mx = std::max<long long>(n1, n2) + 1;
+    const int blocks = (int)std::min<long long>((mx + threads - 1) / threads, 1024);
+    switch (kind) {
+      case K_LCS: degenerate_kernel<K_LCS><<<blocks, threads, 0, st>>>(N, M, sc.ed_rule, d_last_row, d_last_col, d_out); break;
+      case K_ED: degenerate_kernel<K_ED><<<blocks, threads, 0, st>>>(N, M, sc.ed_rule, d_last_row, d_last_col, d_out); break;
+      default: degenerate_kernel<K_SW><<<blocks, threads, 0, st>>>(N, M, sc.ed_rule, d_last_row, d_last_col, d_out); break;
+    }
+    ws.launches += 1;
+    e = cudaGetLastError();
+    return e == cudaSuccess ? ST_OK : ws.fail(e, "degenerate_kernel");
+  }
+  const long long H = (long long)NW * 32 * R;
+  const long long nbands = (n2 + H - 1) / H;
+  if (grid <= 0 || grid > nbands) grid = (int)std::min<long long>(nbands, ws.sms);
+  const int nslot = grid + 2;
+  const long long stride = ((n1 + 1 + 3) / 4) * 4 + 4;
+  const long long a_pad_len = PADL + n1 + PADR;
+  const long long b_pad_len = nbands * H;
+  int rc = ws.reserve(a_pad_len, b_pad_len, (long long)nslot * stride, grid);
+  if (rc != ST_OK) return rc;
+  // unique 32-bit tags per band since the slots were last cleared
+  if ((unsigned long long)ws.tag_next + (unsigned long long)nbands + 2ull >= 0xffffffffull) {
+    e = cudaMemsetAsync(ws.slots, 0, ws.slots_bytes, st);
+    if (e != cudaSuccess) return ws.fail(e, "cudaMemsetAsync(slots)");
+    ws.tag_next = 1;
+  }
+  const unsigned tag0 = ws.tag_next;
+  ws.tag_next += (unsigned)nbands + 1;
+
+  {
+    const int threads = 256;
+    const long long mx = std::max(a_pad_len, b_pad_len);
+    const int blocks = (int)std::min<long long>((mx + threads - 1) / threads, 2 * ws.sms);
+    stage_kernel<<<blocks, threads, 0, st>>>(d_a, N, d_b, M, ws.a_pad, a_pad_len, ws.b_pad, b_pad_len);
+    ws.launches += 1;
+    if ((e = cudaGetLastError()) != cudaSuccess) return ws.fail(e, "stage_kernel");
+  }
+  if ((e = cudaMemsetAsync(ws.ctrl, 0, 4 * sizeof(int), st)) != cudaSuccess)
+    return ws.fail(e, "cudaMemsetAsync(ctrl)");
+
+  PlainParams P;
+  P.a_pad = ws.a_pad;
+  P.b_pad = ws.b_pad;
+  P.N = N;
+  P.M = M;
+  P.H = (int)H;
+  P.nbands = (int)nbands;
+  P.nslot = nslot;
+  P.slot_stride = stride;
+  P.slots = ws.slots;
+  P.tag0 = tag0;
+  P.ctrl = ws.ctrl;
+  P.last_col = d_last_col;
+  P.best = reinterpret_cast<SwBest *>(ws.best);
+  P.sc = sc;
+  P.timeout_ns = timeout_ns;
+  switch (kind) {
+    case K_LCS: e = launch_plain_k<K_LCS>(R, NW, P, grid, st); break;
+    case K_ED: e = launch_plain_k<K_ED>(R, NW, P, grid, st); break;
+    default: e = launch_plain_k<K_SW>(R, NW, P, grid, st); break;
+  }
+  ws.launches += 1;
+  if (e != cudaSuccess) return ws.fail(e, "plain_kernel");
+
+  const unsigned long long *last_slot = ws.slots + (long long)((nbands - 1) % nslot) * stride;
+  if (d_last_row) {
+    const int threads = 256;
+    const int blocks = (int)((n1 + 1 + threads - 1) / threads);
+    switch (kind) {
+      case K_LCS: finish_row_kernel<K_LCS><<<blocks, threads, 0, st>>>(last_slot, N, M, d_last_row); break;
+      case K_ED: finish_row_kernel<K_ED><<<blocks, threads, 0, st>>>(last_slot, N, M, d_last_row); break;
+      default: finish_row_kernel<K_SW><<<blocks, threads, 0, st>>>(last_slot, N, M, d_last_row); break;
+    }
+    ws.launches += 1;
+    if ((e = cudaGetLastError()) != cudaSuccess) return ws.fail(e, "finish_row_kernel");
+  }
+  switch (kind) {
+    case K_LCS: finish_result_kernel<K_LCS><<<1, 256, 0, st>>>(last_slot, N, M, sc.ed_rule, P.best, grid, ws.ctrl, d_out, d_last_col); break;
+    case K_ED: finish_result_kernel<K_ED><<<1, 256, 0, st>>>(last_slot, N, M, sc.ed_rule, P.best, grid, ws.ctrl, d_out, d_last_col); break;
+    default: finish_result_kernel<K_SW><<<1, 256, 0, st>>>(last_slot, N, M, sc.ed_rule, P.best, grid, ws.ctrl, d_out, d_last_col); break;
+  }
+  ws.launches += 1;
+  if ((e = cudaGetLastError()) != cudaSuccess) return ws.fail(e, "finish_result_kernel");
+  return ST_OK;
+}
+
+}  // namespace gme

@@ -1,0 +1,46 @@
+// gme_reference.cpp -- the reference's host-function signatures (include/gme_reference.h)
+// implemented on the C ABI.
+#include <climits>
+#include <mutex>
+
+#include "../../include/gme_reference.h"
+
+namespace {
+std::mutex g_mu;
+gme_context *g_ctx = nullptr;
+thread_local gme_status g_last = GME_OK;
+
+int32_t run(gme_kind kind, int32_t n1, int32_t n2, const int32_t *a, const int32_t *b) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_ctx) {
+    gme_status s = gme_create(0, &g_ctx);
+    if (s != GME_OK) {
+      g_ctx = nullptr;
+      g_last = s;
+      return INT_MIN;
+    }
+  }
+  gme_scoring sc = gme_default_scoring();
+  sc.ed_boundary = GME_ED_STANDARD;  // GPU_setInit
+  gme_result r;
+  gme_status s = gme_align(g_ctx, kind, a, n1, b, n2, &sc, &r, nullptr, nullptr);
+  g_last = s;
+  return s == GME_OK ? r.score : INT_MIN;
+}
+}  // namespace
+
+int LCS(int n1, int n2, int *arr1, int *arr2, int, int, int *) { return run(GME_LCS, n1, n2, arr1, arr2); }
+int LCS(int n1, int n2, int *arr1, int *arr2) { return run(GME_LCS, n1, n2, arr1, arr2); }
+int ED(int n1, int n2, int *arr1, int *arr2, int, int, int *, int, int) { return run(GME_ED, n1, n2, arr1, arr2); }
+int ED(int n1, int n2, int *arr1, int *arr2, int, int, int *) { return run(GME_ED, n1, n2, arr1, arr2); }
+int ED(int n1, int n2, int *arr1, int *arr2) { return run(GME_ED, n1, n2, arr1, arr2); }
+int SW(int n1, int n2, int *arr1, int *arr2, int, int, int *, int, int) { return run(GME_SW, n1, n2, arr1, arr2); }
+int SW(int n1, int n2, int *arr1, int *arr2, int, int, int *) { return run(GME_SW, n1, n2, arr1, arr2); }
+int SW(int n1, int n2, int *arr1, int *arr2) { return run(GME_SW, n1, n2, arr1, arr2); }
+
+extern "C" {
+gme_status gme_reference_last_status(void) { return g_last; }
+int32_t gme_ref_lcs(int32_t n1, int32_t n2, const int32_t *a, const int32_t *b) { return run(GME_LCS, n1, n2, a, b); }
+int32_t gme_ref_ed(int32_t n1, int32_t n2, const int32_t *a, const int32_t *b) { return run(GME_ED, n1, n2, a, b); }
+int32_t gme_ref_sw(int32_t n1, int32_t n2, const int32_t *a, const int32_t *b) { return run(GME_SW, n1, n2, a, b); }
+}

@@ -1,0 +1,129 @@
+/*
+ * gme.h -- C ABI of the GB300 wavefront alignment library (libgme.so).
+ *
+ * Three integer dynamic programs over two integer-coded sequences, exactly as
+ * the reference computes them:
+ *   LCS  t = a==b ? diag+1 : max(left, up)                 LCS/LCS.cpp:59-63
+ *   ED   t = a==b ? diag : min(up,left,diag)+1             EditDistance/ED.cpp:63-65
+ *   SW   t = max(left+gap, up+gap, diag+(a==b?match:mismatch), 0)
+ *                                                          SmithWaterman/SW.cpp:45-47,63-65
+ * Table convention (the reference's GPU host functions, e.g.
+ * EditDistance/GPU_Hyperlane_Share.cu:696-697): columns x = 0..n1 run over
+ * `a` (arr1), rows y = 0..n2 run over `b` (arr2), cell (y,x) compares
+ * a[x-1] with b[y-1].  The returned score is the bottom-right cell (y=n2,
+ * x=n1), which is what every reference host function returns.
+ *
+ * Plain pointers and sizes only; no C++ or CUDA types appear in signatures
+ * (streams are passed as void* holding a cudaStream_t).  Every function returns
+ * a gme_status; nothing in this library calls exit() (the reference's
+ * checkGPUError does, EditDistance/GPU_Hyperlane_Share.cu:682-687).
+ *
+ * The reference's own C++ signatures (int ED(int,int,int*,int*,int,int,int*,int,int)
+ * and friends) are provided on top of this ABI by gme_reference.h.
+ */
+#ifndef GME_H
+#define GME_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gme_status {
+  GME_OK = 0,
+  GME_ERR_INVALID = 1,   /* bad argument (null pointer, negative size, bad kind) */
+  GME_ERR_CUDA = 2,      /* a CUDA runtime call failed; see gme_last_error() */
+  GME_ERR_NOMEM = 3,     /* device or pinned allocation failed */
+  GME_ERR_TIMEOUT = 4,   /* a bounded device-side wait expired; results invalid */
+  GME_ERR_OVERFLOW = 5,  /* sizes whose scores could overflow int32 */
+  GME_ERR_BUDGET = 6,    /* served path: request larger than the HBM budget */
+  GME_ERR_NOT_READY = 7, /* served path: ticket still in flight */
+  GME_ERR_CLOSED = 8     /* served path: server shut down */
+} gme_status;
+
+typedef enum gme_kind { GME_LCS = 0, GME_ED = 1, GME_SW = 2 } gme_kind;
+
+/* Edit-distance boundary (row 0 / column 0) convention. */
+typedef enum gme_ed_boundary {
+  /* EditDistance/ED.cpp:48-54 (the CPU oracle): row 0 = [0,0,1,2,...,n1-1],
+   * column 0 = [0,1,...,n2]. */
+  GME_ED_REF_CPU = 0,
+  /* GPU_setInit, EditDistance/GPU_Hyperlane_Share.cu:16-22: row 0 = [0,1,...,n1],
+   * column 0 = [0,1,...,n2] (textbook Levenshtein). */
+  GME_ED_STANDARD = 1
+} gme_ed_boundary;
+
+/* Scoring constants.  A zeroed struct is NOT valid for SW; use gme_default_scoring(). */
+typedef struct gme_scoring {
+  int32_t match;       /* SW: added on a[x-1]==b[y-1]          (SW.cpp:46: +3) */
+  int32_t mismatch;    /* SW: added otherwise                  (SW.cpp:46: -3) */
+  int32_t gap;         /* SW: added to left and up             (SW.cpp:63-64: -2) */
+  int32_t ed_boundary; /* ED: a gme_ed_boundary value */
+} gme_scoring;
+
+typedef struct gme_result {
+  int32_t score;    /* bottom-right cell (all kinds) */
+  int32_t sw_max;   /* SW: largest cell; 0 when no cell is positive */
+  int64_t sw_max_y; /* SW: its row (1-based, over b); first maximum in row-major order; 0 if none */
+  int64_t sw_max_x; /* SW: its column (1-based, over a) */
+  int32_t status;   /* device-side status of the computation (a gme_status) */
+  int32_t kind;     /* echo of the kind computed */
+} gme_result;
+
+/* Tuning of the plain (one pair per call) wavefront kernel. Zero fields = automatic. */
+typedef struct gme_plain_config {
+  int32_t rows_per_lane;   /* cells of one anti-diagonal held per thread: 4 or 8 */
+  int32_t warps_per_band;  /* compute warps per CTA; band height = warps*32*rows_per_lane */
+  int32_t grid;            /* persistent CTAs (0 = one per band, capped by residency) */
+  int32_t reserved;
+} gme_plain_config;
+
+typedef struct gme_context gme_context;
+
+/* ---- context ---------------------------------------------------------------- */
+/* A context owns a device, a workspace that grows on demand and is reused across
+ * calls, and host staging buffers.  One context must not be used by two host
+ * threads at once; separate contexts are independent. */
+gme_status gme_create(int device, gme_context **ctx);
+gme_status gme_destroy(gme_context *ctx);
+const char *gme_status_string(gme_status s);
+/* Text of the last error recorded on this context (never NULL). */
+const char *gme_last_error(const gme_context *ctx);
+gme_scoring gme_default_scoring(void);
+/* Upper bound, in nanoseconds, of every device-side spin-wait (default 10 s). */
+gme_status gme_set_wait_timeout_ns(gme_context *ctx, uint64_t ns);
+gme_status gme_set_plain_config(gme_context *ctx, const gme_plain_config *cfg);
+gme_status gme_get_plain_config(const gme_context *ctx, int64_t n1, int64_t n2,
+                                gme_plain_config *resolved);
+
+/* ---- plain path: one alignment per call ------------------------------------- */
+/* Host buffers in and out (the reference host functions' contract: they take
+ * host arrays and return the last cell, e.g. EditDistance/GPU_Hyperlane_Share.cu:689).
+ * last_row (n1+1 values, row y=n2) and last_col (n2+1 values, column x=n1)
+ * are optional (NULL).  Blocks until done. */
+gme_status gme_align(gme_context *ctx, gme_kind kind, const int32_t *a, int64_t n1,
+                     const int32_t *b, int64_t n2, const gme_scoring *sc, gme_result *out,
+                     int32_t *last_row, int32_t *last_col);
+
+/* Device buffers in and out, asynchronous on `stream`.  d_out is a device
+ * gme_result; its `status` field reports a device-side timeout. */
+gme_status gme_align_device(gme_context *ctx, gme_kind kind, const int32_t *d_a, int64_t n1,
+                            const int32_t *d_b, int64_t n2, const gme_scoring *sc,
+                            gme_result *d_out, int32_t *d_last_row, int32_t *d_last_col,
+                            void *stream);
+
+/* ---- diagnostics ------------------------------------------------------------- */
+/* Runs the bounded device wait on a flag that nothing sets and reports what the
+ * kernel returned (expected GME_ERR_TIMEOUT after `timeout_ns`).  Tests use it to
+ * show a wait that runs out ends with a status, not a hang. */
+gme_status gme_debug_wait_timeout(gme_context *ctx, uint64_t timeout_ns, int32_t *kernel_status);
+/* Number of kernels this context launched since creation (the bench counts them). */
+int64_t gme_launch_count(const gme_context *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GME_H */
