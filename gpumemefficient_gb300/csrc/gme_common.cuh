@@ -114,6 +114,7 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 // the block-wide abort word and the grid-wide status word are checked.
 // Returns false (after recording ST_TIMEOUT in *status) when the deadline passes
 // or another warp has already given up; the caller then abandons its work.
+// Called by all 32 lanes of a warp; poll() must return the same value in each.
 struct Waiter {
   unsigned long long timeout, deadline;
   int *status;          // global status word (0 = fine)
@@ -127,10 +128,14 @@ struct Waiter {
     unsigned it = 0;
     while (!poll()) {
       if ((++it & 63u) == 0) {
-        if (*abort) return false;
-        if (ld_relaxed_gpu_s32(status) != 0) { *abort = 1; return false; }
-        if (globaltimer_ns() > deadline) {
-          atomicCAS(status, 0, ST_TIMEOUT);
+        // decide once per warp so that every lane leaves the loop together
+        int give = 0;
+        if (*abort) give = 1;
+        else if (ld_relaxed_gpu_s32(status) != 0) give = 2;
+        else if (globaltimer_ns() > deadline) give = 3;
+        give = __shfl_sync(0xffffffffu, give, 0);
+        if (give) {
+          if (give == 3) atomicCAS(status, 0, ST_TIMEOUT);
           *abort = 1;
           return false;
         }

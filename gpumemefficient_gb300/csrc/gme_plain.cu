@@ -74,14 +74,41 @@ struct PlainParams {
   unsigned long long timeout_ns;
 };
 
+// Rings carry 64-bit entries {tag = column + 1, value}: a consumer knows an entry
+// is the one it wants from the entry itself, so no fence or separate progress
+// flag sits between producer and consumer (an acquire/release pair per chunk
+// would also wait for the in-flight symbol prefetch).  Only the consumer's
+// position is published, for back-pressure.  Rings are zeroed when a band starts.
 template <int NW> struct __align__(16) PlainSmem {
-  int ring[NW + 1][RING];
-  int prod[NW + 1];
+  unsigned long long ring[NW + 1][RING];
   int cons[NW + 1];
   int band;
   int abort;
   SwBest best[NW + 1];
 };
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void lds_u64x4(const unsigned long long *p, unsigned long long (&e)[4]) {
+  asm volatile("ld.volatile.shared.v2.u64 {%0,%1}, [%2];" : "=l"(e[0]), "=l"(e[1]) : "r"(smem_addr(p)));
+  asm volatile("ld.volatile.shared.v2.u64 {%0,%1}, [%2+16];" : "=l"(e[2]), "=l"(e[3]) : "r"(smem_addr(p)));
+}
+__device__ __forceinline__ void sts_u64x4(unsigned long long *p, const unsigned long long (&e)[4]) {
+  asm volatile("st.volatile.shared.v2.u64 [%0], {%1,%2};" :: "r"(smem_addr(p)), "l"(e[0]), "l"(e[1]) : "memory");
+  asm volatile("st.volatile.shared.v2.u64 [%0+16], {%1,%2};" :: "r"(smem_addr(p)), "l"(e[2]), "l"(e[3]) : "memory");
+}
+__device__ __forceinline__ int lds_vol(const int *p) {
+  int v;
+  asm volatile("ld.volatile.shared.b32 %0, [%1];" : "=r"(v) : "r"(smem_addr(p)));
+  return v;
+}
+__device__ __forceinline__ void sts_vol(int *p, int v) {
+  asm volatile("st.volatile.shared.b32 [%0], %1;" :: "r"(smem_addr(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long entry(int pos, int v) {
+  return ((unsigned long long)(unsigned)(pos + 1) << 32) | (unsigned)v;
+}
 
 __device__ __forceinline__ int4 ldg4(const int *p) { return __ldg(reinterpret_cast<const int4 *>(p)); }
 
@@ -163,22 +190,33 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
   int4 nextq = ldg4(P.a_pad + base + 4);
 
   int recv = 0, recv_prev = 0;
-  int *ring_in = S.ring[warp];
-  int *ring_out = S.ring[warp + 1];
-  int *prod_in = &S.prod[warp], *cons_in = &S.cons[warp];
-  int *prod_out = &S.prod[warp + 1], *cons_out = &S.cons[warp + 1];
+  unsigned long long *ring_in = S.ring[warp];
+  unsigned long long *ring_out = S.ring[warp + 1];
+  int *cons_in = &S.cons[warp], *cons_out = &S.cons[warp + 1];
+  int cons_seen = 0;
   const int j_end = N / 4 + 8 * R;  // last chunk: lane 31's last row reaches column N
 
   for (int j = 0; j <= j_end; ++j) {
     const int s0 = 4 * j;
     // incoming row (columns 4j..4j+3) for lane 0, read by lane 31
-    const int need = min(s0 + 4, N + 1);
-    if (!W.wait([&] { return ld_acquire_cta(prod_in) >= need; })) return;
     int inv[4] = {0, 0, 0, 0};
-    if (lane == 31) {
-      int4 q = *reinterpret_cast<const int4 *>(&ring_in[s0 & (RING - 1)]);
-      inv[0] = q.x; inv[1] = q.y; inv[2] = q.z; inv[3] = q.w;
+    {
+      auto fetch = [&]() -> bool {
+        bool ok = true;
+        if (lane == 31) {
+          unsigned long long e[4];
+          lds_u64x4(&ring_in[s0 & (RING - 1)], e);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            inv[k] = (int)(unsigned)e[k];
+            if (s0 + k <= N && (unsigned)(e[k] >> 32) != (unsigned)(s0 + k + 1)) ok = false;
+          }
+        }
+        return __shfl_sync(FULL, ok, 31);
+      };
+      if (!W.wait(fetch)) return;
     }
+    if (lane == 31) sts_vol(cons_in, s0 + 4);
     const int4 q_now = nextq;
     nextq = ldg4(P.a_pad + base + 4 * (j + 2));
 
@@ -194,16 +232,22 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
       steps4<KIND, R, true, false>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0, lane, N,
                                    padmask, smax, sstep);
     }
-    if (lane == 31) st_release_cta(cons_in, s0 + 4);
 
     // outgoing row: columns 4jo..4jo+3, jo = j - 8R
     const int jo = j - 8 * R;
     if (jo >= 0) {
       const int pos = 4 * jo;
-      if (!W.wait([&] { return ld_acquire_cta(cons_out) >= pos + 4 - RING; })) return;
+      if (pos + 4 - RING > cons_seen) {
+        if (!W.wait([&] {
+              cons_seen = lds_vol(cons_out);
+              return cons_seen >= pos + 4 - RING;
+            }))
+          return;
+      }
       if (lane == 31) {
-        *reinterpret_cast<int4 *>(&ring_out[pos & (RING - 1)]) = make_int4(outq[0], outq[1], outq[2], outq[3]);
-        st_release_cta(prod_out, pos + 4);
+        const unsigned long long e[4] = {entry(pos, outq[0]), entry(pos + 1, outq[1]),
+                                         entry(pos + 2, outq[2]), entry(pos + 3, outq[3])};
+        sts_u64x4(&ring_out[pos & (RING - 1)], e);
       }
     }
     // slide the symbol window by four columns
@@ -237,8 +281,8 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int ac
   unsigned long long *dst = P.slots + (long long)(band % P.nslot) * P.slot_stride;
   const unsigned src_tag = P.tag0 + (unsigned)(band - 1);
   const unsigned long long dst_tag = (unsigned long long)(P.tag0 + (unsigned)band) << 32;
-  int *ring0 = S.ring[0];
-  int *ringo = S.ring[active];
+  unsigned long long *ring0 = S.ring[0];
+  unsigned long long *ringo = S.ring[active];
   int in_pos = 0, out_pos = 0;
   unsigned idle = 0;
   unsigned long long deadline = 0;
@@ -246,7 +290,7 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int ac
   while (in_pos < N1 || out_pos < N1) {
     bool moved = false;
     if (in_pos < N1) {
-      const int space = RING - (in_pos - ld_acquire_cta(&S.cons[0]));
+      const int space = RING - (in_pos - lds_vol(&S.cons[0]));
       const int want = min(N1 - in_pos, space);
       if (want > 0) {
         const int p = in_pos + 4 * lane;
@@ -276,31 +320,35 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int ac
         const int n = min(4 * lanes_ok, want);
         if (n > 0) {
           if (4 * lane < n) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) ring0[(p + k) & (RING - 1)] = v[k];
+            const unsigned long long e[4] = {entry(p, v[0]), entry(p + 1, v[1]), entry(p + 2, v[2]),
+                                             entry(p + 3, v[3])};
+            sts_u64x4(&ring0[p & (RING - 1)], e);
           }
-          __syncwarp();
-          if (lane == 0) st_release_cta(&S.prod[0], in_pos + n);
           in_pos += n;
           moved = true;
         }
       }
     }
     if (out_pos < N1) {
-      const int avail = min(ld_acquire_cta(&S.prod[active]), N1);
-      const int n = min(avail - out_pos, 128);
+      const int p = out_pos + 4 * lane;
+      unsigned long long e[4];
+      lds_u64x4(&ringo[p & (RING - 1)], e);
+      bool ok = p < N1;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (p + k < N1 && (unsigned)(e[k] >> 32) != (unsigned)(p + k + 1)) ok = false;
+      const unsigned okm = __ballot_sync(FULL, ok);
+      const int lanes_ok = (okm == FULL) ? 32 : (__ffs(~okm) - 1);
+      const int n = min(4 * lanes_ok, N1 - out_pos);
       if (n > 0) {
-        const int p = out_pos + 4 * lane;
         if (4 * lane < n) {
-          const int4 q = *reinterpret_cast<const int4 *>(&ringo[p & (RING - 1)]);
           volatile unsigned long long *dp = dst + p;
-          const unsigned long long w0 = dst_tag | (unsigned)q.x, w1 = dst_tag | (unsigned)q.y;
-          const unsigned long long w2 = dst_tag | (unsigned)q.z, w3 = dst_tag | (unsigned)q.w;
+          const unsigned long long w0 = dst_tag | (unsigned)e[0], w1 = dst_tag | (unsigned)e[1];
+          const unsigned long long w2 = dst_tag | (unsigned)e[2], w3 = dst_tag | (unsigned)e[3];
           asm volatile("st.volatile.global.v2.u64 [%0], {%1,%2};" :: "l"(dp), "l"(w0), "l"(w1) : "memory");
           asm volatile("st.volatile.global.v2.u64 [%0+16], {%1,%2};" :: "l"(dp), "l"(w2), "l"(w3) : "memory");
         }
-        __syncwarp();
-        if (lane == 0) st_release_cta(&S.cons[active], out_pos + n);
+        if (lane == 0) sts_vol(&S.cons[active], out_pos + n);
         out_pos += n;
         moved = true;
       }
@@ -336,8 +384,9 @@ __global__ void __launch_bounds__((NW + 1) * 32, 1) plain_kernel(PlainParams P) 
     if (threadIdx.x == 0) {
       S.band = S.abort ? P.nbands : atomicAdd(&P.ctrl[0], 1);
 #pragma unroll
-      for (int k = 0; k <= NW; ++k) { S.prod[k] = 0; S.cons[k] = 0; }
+      for (int k = 0; k <= NW; ++k) S.cons[k] = 0;
     }
+    for (int i = threadIdx.x; i < (NW + 1) * RING; i += blockDim.x) (&S.ring[0][0])[i] = 0ull;
     __syncthreads();
     const int band = S.band;
     if (band >= P.nbands) break;
@@ -466,34 +515,39 @@ static cudaError_t launch_plain_k(int R, int NW, const PlainParams &P, int grid,
     switch (NW) {
       case 1: return launch_plain_t<KIND, 4, 1>(P, grid, st);
       case 2: return launch_plain_t<KIND, 4, 2>(P, grid, st);
+      case 3: return launch_plain_t<KIND, 4, 3>(P, grid, st);
       case 4: return launch_plain_t<KIND, 4, 4>(P, grid, st);
+      case 6: return launch_plain_t<KIND, 4, 6>(P, grid, st);
       case 8: return launch_plain_t<KIND, 4, 8>(P, grid, st);
     }
   } else if (R == 8) {
     switch (NW) {
       case 1: return launch_plain_t<KIND, 8, 1>(P, grid, st);
       case 2: return launch_plain_t<KIND, 8, 2>(P, grid, st);
+      case 3: return launch_plain_t<KIND, 8, 3>(P, grid, st);
       case 4: return launch_plain_t<KIND, 8, 4>(P, grid, st);
-      case 8: return launch_plain_t<KIND, 8, 8>(P, grid, st);
     }
   }
   return cudaErrorInvalidValue;
 }
 
 bool plain_config_valid(int R, int NW) {
-  return (R == 4 || R == 8) && (NW == 1 || NW == 2 || NW == 4 || NW == 8);
+  if (R == 4) return NW == 1 || NW == 2 || NW == 3 || NW == 4 || NW == 6 || NW == 8;
+  if (R == 8) return NW >= 1 && NW <= 4;
+  return false;
 }
 
-// Automatic shape: enough bands to cover the SMs, as few band boundaries as
-// possible (each costs one L2 hand-off on the critical path).
+// Automatic shape.  Every band boundary costs one L2 hand-off on the critical
+// path and a band that has to wait for a free CTA doubles the sweep, so take the
+// shortest band (most SMs busy) for which all bands run at once, one per SM.
 void plain_auto_config(int sms, long long n1, long long n2, int *R, int *NW, int *grid) {
   (void)n1;
-  int r = 4, nw = 4;
-  const long long rows_per_sm = (n2 + sms - 1) / sms;
-  if (rows_per_sm >= 8 * 32 * 4) { r = 8; nw = 8; }
-  else if (rows_per_sm >= 4 * 32 * 4) { r = 4; nw = 4; }
-  else if (rows_per_sm >= 2 * 32 * 4) { r = 4; nw = 2; }
-  else { r = 4; nw = 1; }
+  static const int cand[][2] = {{4, 1}, {4, 2}, {4, 3}, {4, 4}, {4, 6}, {4, 8}};
+  int r = 4, nw = 8;
+  for (const auto &c : cand) {
+    const long long H = (long long)c[1] * 32 * c[0];
+    if ((n2 + H - 1) / H <= sms) { r = c[0]; nw = c[1]; break; }
+  }
   *R = r;
   *NW = nw;
   const long long H = (long long)nw * 32 * r;
