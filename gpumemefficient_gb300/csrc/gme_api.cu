@@ -260,7 +260,7 @@ gme_status gme_set_plain_config(gme_context *ctx, const gme_plain_config *cfg) {
   if (!cfg) { ctx->cfg = gme_plain_config{}; return GME_OK; }
   if ((cfg->rows_per_lane || cfg->warps_per_band) &&
       !gme::plain_config_valid(cfg->rows_per_lane, cfg->warps_per_band)) {
-    ctx->ws.last_error = "plain config: rows_per_lane must be 4 or 8, warps_per_band 1, 2, 4 or 8";
+    ctx->ws.last_error = "plain config: rows_per_lane 4 with warps_per_band 1,2,3,4,6,8, or rows_per_lane 8 with 1..4";
     return GME_ERR_INVALID;
   }
   if (cfg->grid < 0) return GME_ERR_INVALID;

@@ -113,30 +113,39 @@ __device__ __forceinline__ unsigned long long entry(int pos, int v) {
 __device__ __forceinline__ int4 ldg4(const int *p) { return __ldg(reinterpret_cast<const int4 *>(p)); }
 
 // ---------------------------------------------------------------------------
-// Four wavefront steps of one lane (R rows).  CHECKED: some cells of the warp
-// fall outside 1 <= x <= N (ramp-in/out) and hold their value.  PADROWS: rows
-// beyond n2 copy the row above, so the warp's bottom row equals row n2.
+// Four wavefront steps of one lane (R rows).
+//
+// State entering step s: cur[r] = cells after step s-1, prv[r] = after step s-2,
+// recv = the cell above row 0 for step s (lane t: lane t-1's bottom cell after
+// step s-1; lane 0: the incoming row at column s), recv_prev = recv of step s-1.
+// The diagonal terms need only values two steps old, so they are formed first;
+// the bottom row is computed next and shuffled to the lane below at once, and
+// the other rows are computed while the shuffle is in flight.
+//
+// CHECKED: some cells of the warp fall outside 1 <= x <= n1 (ramp-in/out) and
+// hold their value.  PADROWS: rows beyond n2 copy the row above, so the warp's
+// bottom row equals row n2.
 // ---------------------------------------------------------------------------
 template <int KIND, int R, bool CHECKED, bool PADROWS>
 __device__ __forceinline__ void steps4(const Rec<KIND> &rec, int (&cur)[R], int (&prv)[R],
                                        int &recv, int &recv_prev, const int (&win)[R + 4],
-                                       const int (&bs)[R], const int (&inv)[4], int (&outq)[4],
+                                       const int (&bs)[R], const int (&inv)[5], int (&outq)[4],
                                        int s0, int lane, int N, unsigned padmask,
                                        int (&smax)[R], int (&sstep)[R]) {
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int s = s0 + q;
-    const int send = (lane == 31) ? inv[q] : cur[R - 1];
     outq[q] = cur[R - 1];  // lane 31: bottom cell after step s-1 (column s-32R)
-    recv_prev = recv;
-    recv = __shfl_sync(FULL, send, (lane + 31) & 31);
+    int D[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      D[r] = (r ? prv[r - 1] : recv_prev) + (win[R + q - r] == bs[r] ? rec.ceq : rec.cne);
     int nv[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
+    for (int k = 0; k < R; ++k) {
+      const int r = (k == 0) ? R - 1 : k - 1;  // bottom row first
       const int up = r ? cur[r - 1] : recv;
-      const int dg = r ? prv[r - 1] : recv_prev;
-      const int D = dg + (win[R + q - r] == bs[r] ? rec.ceq : rec.cne);
-      int v = rec.cell(up, cur[r], D);
+      int v = rec.cell(up, cur[r], D[r]);
       if (CHECKED) {
         const int x = s - lane * R - r;
         if ((unsigned)(x - 1) >= (unsigned)N) v = cur[r];
@@ -148,6 +157,13 @@ __device__ __forceinline__ void steps4(const Rec<KIND> &rec, int (&cur)[R], int 
         if (v > smax[r]) { smax[r] = v; sstep[r] = s; }
       }
       nv[r] = v;
+      if (k == 0) {
+        // lane 31 feeds the incoming row's next column to lane 0 through the same shuffle
+        const int send = (lane == 31) ? inv[q + 1] : v;
+        const int nxt = __shfl_sync(FULL, send, (lane + 31) & 31);
+        recv_prev = recv;
+        recv = nxt;  // rows r >= 1 below use cur[], not recv
+      }
     }
 #pragma unroll
     for (int r = 0; r < R; ++r) { prv[r] = cur[r]; cur[r] = nv[r]; }
@@ -155,9 +171,11 @@ __device__ __forceinline__ void steps4(const Rec<KIND> &rec, int (&cur)[R], int 
 }
 
 // One compute warp sweeping its 32*R rows of a band across all N columns.
+// Warps hand their bottom row to the next warp through a shared ring; the last
+// active warp of the band writes it straight to the band's global slot.
 template <int KIND, int R, int NW>
 __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, int warp, int lane,
-                             Waiter &W, SwBest &tb) {
+                             int active, Waiter &W, SwBest &tb) {
   const Rec<KIND> rec(P.sc);
   const int N = P.N, M = P.M;
   const int yl = band * P.H + warp * 32 * R + lane * R + 1;  // first row of this lane
@@ -177,6 +195,7 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
     if (yl + r > M) padmask |= 1u << r;
   }
   const bool padwarp = __any_sync(FULL, padmask != 0);
+  const bool last = (warp == active - 1);
 
   // Symbol window: win[k] = a_pad[base + 4j - R + k]; the symbol of row r at
   // step 4j+q is win[R+q-r] (column x = 4j+q - lane*R - r, a[x-1]).
@@ -189,34 +208,53 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
   }
   int4 nextq = ldg4(P.a_pad + base + 4);
 
-  int recv = 0, recv_prev = 0;
-  unsigned long long *ring_in = S.ring[warp];
+  const unsigned long long *ring_in = S.ring[warp];
   unsigned long long *ring_out = S.ring[warp + 1];
   int *cons_in = &S.cons[warp], *cons_out = &S.cons[warp + 1];
+  unsigned long long *gdst = P.slots + (long long)(band % P.nslot) * P.slot_stride;
+  const unsigned long long gtag = (unsigned long long)(P.tag0 + (unsigned)band) << 32;
   int cons_seen = 0;
   const int j_end = N / 4 + 8 * R;  // last chunk: lane 31's last row reaches column N
 
+  // Incoming row, chunk j = columns 4j..4j+3.  Every lane reads the same four
+  // entries (a broadcast) so that every lane can check the tags itself.
+  auto valid = [&](const unsigned long long (&e)[4], int p0) {
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (p0 + k <= N && (unsigned)(e[k] >> 32) != (unsigned)(p0 + k + 1)) ok = false;
+    return ok;
+  };
+  unsigned long long e_cur[4], e_nxt[4];
+  if (!W.wait([&] {
+        lds_u64x4(&ring_in[0], e_cur);
+        return valid(e_cur, 0);
+      }))
+    return;
+  lds_u64x4(&ring_in[4 & (RING - 1)], e_nxt);
+  int recv_prev = 0;
+  int recv = __shfl_sync(FULL, (lane == 31) ? (int)(unsigned)e_cur[0] : cur[R - 1], (lane + 31) & 31);
+
   for (int j = 0; j <= j_end; ++j) {
     const int s0 = 4 * j;
-    // incoming row (columns 4j..4j+3) for lane 0, read by lane 31
-    int inv[4] = {0, 0, 0, 0};
-    {
-      auto fetch = [&]() -> bool {
-        bool ok = true;
-        if (lane == 31) {
-          unsigned long long e[4];
-          lds_u64x4(&ring_in[s0 & (RING - 1)], e);
+    if (j > 0) {
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            inv[k] = (int)(unsigned)e[k];
-            if (s0 + k <= N && (unsigned)(e[k] >> 32) != (unsigned)(s0 + k + 1)) ok = false;
-          }
-        }
-        return __shfl_sync(FULL, ok, 31);
-      };
-      if (!W.wait(fetch)) return;
+      for (int k = 0; k < 4; ++k) e_cur[k] = e_nxt[k];
+      if (!valid(e_cur, s0)) {
+        // the prefetch ran ahead of the producer: wait, then repair what lane 0
+        // was sent for this chunk's first step
+        if (!W.wait([&] {
+              lds_u64x4(&ring_in[s0 & (RING - 1)], e_cur);
+              return valid(e_cur, s0);
+            }))
+          return;
+        if (lane == 0) recv = (int)(unsigned)e_cur[0];
+      }
+      lds_u64x4(&ring_in[(s0 + 4) & (RING - 1)], e_nxt);
     }
     if (lane == 31) sts_vol(cons_in, s0 + 4);
+    const int inv[5] = {(int)(unsigned)e_cur[0], (int)(unsigned)e_cur[1], (int)(unsigned)e_cur[2],
+                        (int)(unsigned)e_cur[3], (int)(unsigned)e_nxt[0]};
     const int4 q_now = nextq;
     nextq = ldg4(P.a_pad + base + 4 * (j + 2));
 
@@ -234,20 +272,29 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
     }
 
     // outgoing row: columns 4jo..4jo+3, jo = j - 8R
-    const int jo = j - 8 * R;
-    if (jo >= 0) {
-      const int pos = 4 * jo;
-      if (pos + 4 - RING > cons_seen) {
-        if (!W.wait([&] {
-              cons_seen = lds_vol(cons_out);
-              return cons_seen >= pos + 4 - RING;
-            }))
-          return;
-      }
-      if (lane == 31) {
-        const unsigned long long e[4] = {entry(pos, outq[0]), entry(pos + 1, outq[1]),
-                                         entry(pos + 2, outq[2]), entry(pos + 3, outq[3])};
-        sts_u64x4(&ring_out[pos & (RING - 1)], e);
+    const int pos = s0 - 32 * R;
+    if (pos >= 0) {
+      if (last) {
+        if (lane == 31) {
+          volatile unsigned long long *dp = gdst + pos;
+          const unsigned long long w0 = gtag | (unsigned)outq[0], w1 = gtag | (unsigned)outq[1];
+          const unsigned long long w2 = gtag | (unsigned)outq[2], w3 = gtag | (unsigned)outq[3];
+          asm volatile("st.volatile.global.v2.u64 [%0], {%1,%2};" :: "l"(dp), "l"(w0), "l"(w1) : "memory");
+          asm volatile("st.volatile.global.v2.u64 [%0+16], {%1,%2};" :: "l"(dp), "l"(w2), "l"(w3) : "memory");
+        }
+      } else {
+        if (pos + 4 - RING > cons_seen) {
+          if (!W.wait([&] {
+                cons_seen = lds_vol(cons_out);
+                return cons_seen >= pos + 4 - RING;
+              }))
+            return;
+        }
+        if (lane == 31) {
+          const unsigned long long e[4] = {entry(pos, outq[0]), entry(pos + 1, outq[1]),
+                                           entry(pos + 2, outq[2]), entry(pos + 3, outq[3])};
+          sts_u64x4(&ring_out[pos & (RING - 1)], e);
+        }
       }
     }
     // slide the symbol window by four columns
@@ -270,86 +317,58 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
   }
 }
 
-// The I/O warp of a band: incoming row (global -> ring 0) and outgoing row
-// (ring `active` -> global), each lane moving four consecutive columns.
+// The I/O warp of a band: forwards the band's incoming row into ring 0, each
+// lane moving four consecutive columns per round.  Band 0 reads the table's top
+// border; later bands poll the tagged words of the band above (one L2 round
+// trip per poll, no flag).
 template <int KIND, int NW>
-__device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int active, int lane,
-                        Waiter &W) {
+__device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int lane) {
   const int N1 = P.N + 1;
   const unsigned long long *src =
       band > 0 ? P.slots + (long long)((band - 1) % P.nslot) * P.slot_stride : nullptr;
-  unsigned long long *dst = P.slots + (long long)(band % P.nslot) * P.slot_stride;
   const unsigned src_tag = P.tag0 + (unsigned)(band - 1);
-  const unsigned long long dst_tag = (unsigned long long)(P.tag0 + (unsigned)band) << 32;
   unsigned long long *ring0 = S.ring[0];
-  unsigned long long *ringo = S.ring[active];
-  int in_pos = 0, out_pos = 0;
+  int in_pos = 0;
   unsigned idle = 0;
   unsigned long long deadline = 0;
 
-  while (in_pos < N1 || out_pos < N1) {
+  while (in_pos < N1) {
     bool moved = false;
-    if (in_pos < N1) {
-      const int space = RING - (in_pos - lds_vol(&S.cons[0]));
-      const int want = min(N1 - in_pos, space);
-      if (want > 0) {
-        const int p = in_pos + 4 * lane;
-        int v[4] = {0, 0, 0, 0};
-        bool ok = true;
-        if (4 * lane < want) {
-          if (band == 0) {
+    const int space = RING - (in_pos - lds_vol(&S.cons[0]));
+    const int want = min(N1 - in_pos, space);
+    if (want > 0) {
+      const int p = in_pos + 4 * lane;
+      int v[4] = {0, 0, 0, 0};
+      bool ok = true;
+      if (4 * lane < want) {
+        if (band == 0) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) v[k] = Rec<KIND>::top(p + k, P.sc.ed_rule);
-          } else {
-            const volatile unsigned long long *sp = src + p;
-            unsigned long long w0, w1, w2, w3;
-            asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2];" : "=l"(w0), "=l"(w1) : "l"(sp));
-            asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2+16];" : "=l"(w2), "=l"(w3) : "l"(sp));
-            const unsigned long long w[4] = {w0, w1, w2, w3};
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              v[k] = (int)(unsigned)w[k];
-              if (p + k < N1 && (unsigned)(w[k] >> 32) != src_tag) ok = false;
-            }
-          }
+          for (int k = 0; k < 4; ++k) v[k] = Rec<KIND>::top(p + k, P.sc.ed_rule);
         } else {
-          ok = false;
-        }
-        const unsigned okm = __ballot_sync(FULL, ok);
-        const int lanes_ok = (okm == FULL) ? 32 : (__ffs(~okm) - 1);
-        const int n = min(4 * lanes_ok, want);
-        if (n > 0) {
-          if (4 * lane < n) {
-            const unsigned long long e[4] = {entry(p, v[0]), entry(p + 1, v[1]), entry(p + 2, v[2]),
-                                             entry(p + 3, v[3])};
-            sts_u64x4(&ring0[p & (RING - 1)], e);
-          }
-          in_pos += n;
-          moved = true;
-        }
-      }
-    }
-    if (out_pos < N1) {
-      const int p = out_pos + 4 * lane;
-      unsigned long long e[4];
-      lds_u64x4(&ringo[p & (RING - 1)], e);
-      bool ok = p < N1;
+          const volatile unsigned long long *sp = src + p;
+          unsigned long long w0, w1, w2, w3;
+          asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2];" : "=l"(w0), "=l"(w1) : "l"(sp));
+          asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2+16];" : "=l"(w2), "=l"(w3) : "l"(sp));
+          const unsigned long long w[4] = {w0, w1, w2, w3};
 #pragma unroll
-      for (int k = 0; k < 4; ++k)
-        if (p + k < N1 && (unsigned)(e[k] >> 32) != (unsigned)(p + k + 1)) ok = false;
+          for (int k = 0; k < 4; ++k) {
+            v[k] = (int)(unsigned)w[k];
+            if (p + k < N1 && (unsigned)(w[k] >> 32) != src_tag) ok = false;
+          }
+        }
+      } else {
+        ok = false;
+      }
       const unsigned okm = __ballot_sync(FULL, ok);
       const int lanes_ok = (okm == FULL) ? 32 : (__ffs(~okm) - 1);
-      const int n = min(4 * lanes_ok, N1 - out_pos);
+      const int n = min(4 * lanes_ok, want);
       if (n > 0) {
         if (4 * lane < n) {
-          volatile unsigned long long *dp = dst + p;
-          const unsigned long long w0 = dst_tag | (unsigned)e[0], w1 = dst_tag | (unsigned)e[1];
-          const unsigned long long w2 = dst_tag | (unsigned)e[2], w3 = dst_tag | (unsigned)e[3];
-          asm volatile("st.volatile.global.v2.u64 [%0], {%1,%2};" :: "l"(dp), "l"(w0), "l"(w1) : "memory");
-          asm volatile("st.volatile.global.v2.u64 [%0+16], {%1,%2};" :: "l"(dp), "l"(w2), "l"(w3) : "memory");
+          const unsigned long long e[4] = {entry(p, v[0]), entry(p + 1, v[1]), entry(p + 2, v[2]),
+                                           entry(p + 3, v[3])};
+          sts_u64x4(&ring0[p & (RING - 1)], e);
         }
-        if (lane == 0) sts_vol(&S.cons[active], out_pos + n);
-        out_pos += n;
+        in_pos += n;
         moved = true;
       }
     }
@@ -358,16 +377,20 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int ac
     } else {
       // bounded wait: nothing could move this round
       if (idle == 0) deadline = globaltimer_ns() + P.timeout_ns;
-      if ((++idle & 63u) == 0) {
-        if (S.abort) return;
-        if (ld_relaxed_gpu_s32(&P.ctrl[1]) != 0) { S.abort = 1; return; }
-        if (globaltimer_ns() > deadline) {
-          atomicCAS(&P.ctrl[1], 0, ST_TIMEOUT);
+      if ((++idle & 15u) == 0) {
+        int give = 0;
+        if (S.abort) give = 1;
+        else if (ld_relaxed_gpu_s32(&P.ctrl[1]) != 0) give = 2;
+        else if (globaltimer_ns() > deadline) give = 3;
+        give = __shfl_sync(FULL, give, 0);
+        if (give) {
+          if (give == 3) atomicCAS(&P.ctrl[1], 0, ST_TIMEOUT);
           S.abort = 1;
           return;
         }
       }
-      __nanosleep(64);
+      // a full ring waits on the compute warps; an empty poll already cost an L2 round trip
+      if (want <= 0) __nanosleep(256);
     }
   }
 }
@@ -393,9 +416,9 @@ __global__ void __launch_bounds__((NW + 1) * 32, 1) plain_kernel(PlainParams P) 
     const int rows_left = P.M - band * P.H;
     const int active = min(NW, (rows_left + 32 * R - 1) / (32 * R));
     if (warp < NW) {
-      if (warp < active) compute_band<KIND, R, NW>(P, S, band, warp, lane, W, tb);
+      if (warp < active) compute_band<KIND, R, NW>(P, S, band, warp, lane, active, W, tb);
     } else {
-      io_band<KIND, NW>(P, S, band, active, lane, W);
+      io_band<KIND, NW>(P, S, band, lane);
     }
     __syncthreads();
   }
