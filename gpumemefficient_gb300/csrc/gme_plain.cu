@@ -135,6 +135,7 @@ __device__ __forceinline__ void steps4(const Rec<KIND> &rec, int (&cur)[R], int 
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int s = s0 + q;
+    const int rcv = recv;  // the cell above row 0 for this step
     outq[q] = cur[R - 1];  // lane 31: bottom cell after step s-1 (column s-32R)
     int D[R];
 #pragma unroll
@@ -144,7 +145,7 @@ __device__ __forceinline__ void steps4(const Rec<KIND> &rec, int (&cur)[R], int 
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       const int r = (k == 0) ? R - 1 : k - 1;  // bottom row first
-      const int up = r ? cur[r - 1] : recv;
+      const int up = r ? cur[r - 1] : rcv;
       int v = rec.cell(up, cur[r], D[r]);
       if (CHECKED) {
         const int x = s - lane * R - r;
@@ -160,9 +161,8 @@ __device__ __forceinline__ void steps4(const Rec<KIND> &rec, int (&cur)[R], int 
       if (k == 0) {
         // lane 31 feeds the incoming row's next column to lane 0 through the same shuffle
         const int send = (lane == 31) ? inv[q + 1] : v;
-        const int nxt = __shfl_sync(FULL, send, (lane + 31) & 31);
-        recv_prev = recv;
-        recv = nxt;  // rows r >= 1 below use cur[], not recv
+        recv = __shfl_sync(FULL, send, (lane + 31) & 31);  // for step s+1
+        recv_prev = rcv;
       }
     }
 #pragma unroll
