@@ -218,12 +218,16 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
 
   // Incoming row, chunk j = columns 4j..4j+3.  Every lane reads the same four
   // entries (a broadcast) so that every lane can check the tags itself.
+  // Lanes may read a ring word at different moments, so every decision taken on
+  // ring contents is made warp-uniform before anyone acts on it (a lane leaving
+  // a wait alone would strand the others at the next full-warp shuffle).  Equal
+  // tags imply equal values, so lanes that saw valid entries hold the same data.
   auto valid = [&](const unsigned long long (&e)[4], int p0) {
     bool ok = true;
 #pragma unroll
     for (int k = 0; k < 4; ++k)
       if (p0 + k <= N && (unsigned)(e[k] >> 32) != (unsigned)(p0 + k + 1)) ok = false;
-    return ok;
+    return __all_sync(FULL, ok);
   };
   unsigned long long e_cur[4], e_nxt[4];
   if (!W.wait([&] {
@@ -237,6 +241,7 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
 
   for (int j = 0; j <= j_end; ++j) {
     const int s0 = 4 * j;
+    __syncwarp();
     if (j > 0) {
 #pragma unroll
       for (int k = 0; k < 4; ++k) e_cur[k] = e_nxt[k];
@@ -285,7 +290,7 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
       } else {
         if (pos + 4 - RING > cons_seen) {
           if (!W.wait([&] {
-                cons_seen = lds_vol(cons_out);
+                cons_seen = __shfl_sync(FULL, lds_vol(cons_out), 0);
                 return cons_seen >= pos + 4 - RING;
               }))
             return;
@@ -334,7 +339,7 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int la
 
   while (in_pos < N1) {
     bool moved = false;
-    const int space = RING - (in_pos - lds_vol(&S.cons[0]));
+    const int space = RING - (in_pos - __shfl_sync(FULL, lds_vol(&S.cons[0]), 0));
     const int want = min(N1 - in_pos, space);
     if (want > 0) {
       const int p = in_pos + 4 * lane;
