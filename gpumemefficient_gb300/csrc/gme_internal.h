@@ -5,7 +5,7 @@
 #include <stdint.h>
 #include <string>
 
-#include "../../include/gme.h"
+#include "gme.h"
 
 namespace gme {
 

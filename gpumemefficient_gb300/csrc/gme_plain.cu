@@ -43,7 +43,7 @@ namespace gme {
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int RING = 512;   // columns per ring (power of two)
 constexpr int PADL = 261;   // left pad of the staged a[]: >= 32*8+5 and == 1 (mod 4)
-constexpr int PADR = 320;   // right pad (>= 32*8 + 16 + prefetch)
+constexpr int PADR = 352;   // right pad: reads reach base + C*j_end + 2C - 1 <= PADL + N + 32R + 2C
 
 struct SwBest {
   int v;
@@ -113,7 +113,7 @@ __device__ __forceinline__ unsigned long long entry(int pos, int v) {
 __device__ __forceinline__ int4 ldg4(const int *p) { return __ldg(reinterpret_cast<const int4 *>(p)); }
 
 // ---------------------------------------------------------------------------
-// Four wavefront steps of one lane (R rows).
+// C wavefront steps of one lane (R rows): one ring transaction per C steps.
 //
 // State entering step s: cur[r] = cells after step s-1, prv[r] = after step s-2,
 // recv = the cell above row 0 for step s (lane t: lane t-1's bottom cell after
@@ -126,14 +126,16 @@ __device__ __forceinline__ int4 ldg4(const int *p) { return __ldg(reinterpret_ca
 // hold their value.  PADROWS: rows beyond n2 copy the row above, so the warp's
 // bottom row equals row n2.
 // ---------------------------------------------------------------------------
+constexpr int C = 16;  // wavefront steps per ring transaction
+
 template <int KIND, int R, bool CHECKED, bool PADROWS>
-__device__ __forceinline__ void steps4(const Rec<KIND> &rec, int (&cur)[R], int (&prv)[R],
-                                       int &recv, int &recv_prev, const int (&win)[R + 4],
-                                       const int (&bs)[R], const int (&inv)[5], int (&outq)[4],
-                                       int s0, int lane, int N, unsigned padmask,
-                                       int (&smax)[R], int (&sstep)[R]) {
+__device__ __forceinline__ void steps_chunk(const Rec<KIND> &rec, int (&cur)[R], int (&prv)[R],
+                                            int &recv, int &recv_prev, const int (&win)[R + C],
+                                            const int (&bs)[R], const int (&inv)[C], int (&outq)[C],
+                                            int s0, int lane, int N, unsigned padmask,
+                                            int (&smax)[R], int (&sstep)[R]) {
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < C; ++q) {
     const int s = s0 + q;
     const int rcv = recv;  // the cell above row 0 for this step
     outq[q] = cur[R - 1];  // lane 31: bottom cell after step s-1 (column s-32R)
@@ -159,8 +161,10 @@ __device__ __forceinline__ void steps4(const Rec<KIND> &rec, int (&cur)[R], int 
       }
       nv[r] = v;
       if (k == 0) {
-        // lane 31 feeds the incoming row's next column to lane 0 through the same shuffle
-        const int send = (lane == 31) ? inv[q + 1] : v;
+        // lane 31 feeds the incoming row to lane 0 through the same shuffle; the
+        // chunk's last step sends nothing useful: lane 0 re-latches the next
+        // chunk's first column from the validated ring entries
+        const int send = (lane == 31) ? inv[q + 1 < C ? q + 1 : C - 1] : v;
         recv = __shfl_sync(FULL, send, (lane + 31) & 31);  // for step s+1
         recv_prev = rcv;
       }
@@ -197,16 +201,15 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
   const bool padwarp = __any_sync(FULL, padmask != 0);
   const bool last = (warp == active - 1);
 
-  // Symbol window: win[k] = a_pad[base + 4j - R + k]; the symbol of row r at
-  // step 4j+q is win[R+q-r] (column x = 4j+q - lane*R - r, a[x-1]).
+  // Symbol window: win[k] = a_pad[base + s0 - R + k]; the symbol of row r at
+  // step s0+q is win[R+q-r] (column x = s0+q - lane*R - r, a[x-1]).
   const long long base = PADL - 1 - lane * R;
-  int win[R + 4];
+  int win[R + C];
 #pragma unroll
-  for (int k = 0; k < R + 4; k += 4) {
+  for (int k = 0; k < R + C; k += 4) {
     int4 q = ldg4(P.a_pad + base - R + k);
     win[k] = q.x; win[k + 1] = q.y; win[k + 2] = q.z; win[k + 3] = q.w;
   }
-  int4 nextq = ldg4(P.a_pad + base + 4);
 
   const unsigned long long *ring_in = S.ring[warp];
   unsigned long long *ring_out = S.ring[warp + 1];
@@ -214,98 +217,98 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
   unsigned long long *gdst = P.slots + (long long)(band % P.nslot) * P.slot_stride;
   const unsigned long long gtag = (unsigned long long)(P.tag0 + (unsigned)band) << 32;
   int cons_seen = 0;
-  const int j_end = N / 4 + 8 * R;  // last chunk: lane 31's last row reaches column N
+  // last chunk: its output covers column N (outputs lag the inputs by 32R columns)
+  const int j_end = (N + 32 * R) / C;
 
-  // Incoming row, chunk j = columns 4j..4j+3.  Every lane reads the same four
-  // entries (a broadcast) so that every lane can check the tags itself.
-  // Lanes may read a ring word at different moments, so every decision taken on
-  // ring contents is made warp-uniform before anyone acts on it (a lane leaving
-  // a wait alone would strand the others at the next full-warp shuffle).  Equal
-  // tags imply equal values, so lanes that saw valid entries hold the same data.
-  auto valid = [&](const unsigned long long (&e)[4], int p0) {
+  // Incoming row, chunk j = columns Cj..Cj+C-1, as tagged entries {column+1, value}.
+  // Lanes may read a ring word at different moments, so the decision taken on the
+  // entries is made warp-uniform (a lane leaving a wait alone would strand the
+  // others at the next full-warp shuffle).  Equal tags imply equal values.
+  unsigned long long e[C];
+  auto fetch = [&](int p0) {
     bool ok = true;
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
-      if (p0 + k <= N && (unsigned)(e[k] >> 32) != (unsigned)(p0 + k + 1)) ok = false;
+    for (int k = 0; k < C; k += 4) {
+      unsigned long long t[4];
+      lds_u64x4(&ring_in[(p0 + k) & (RING - 1)], t);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        e[k + i] = t[i];
+        if (p0 + k + i <= N && (unsigned)(t[i] >> 32) != (unsigned)(p0 + k + i + 1)) ok = false;
+      }
+    }
     return __all_sync(FULL, ok);
   };
-  unsigned long long e_cur[4], e_nxt[4];
-  if (!W.wait([&] {
-        lds_u64x4(&ring_in[0], e_cur);
-        return valid(e_cur, 0);
-      }))
-    return;
-  lds_u64x4(&ring_in[4 & (RING - 1)], e_nxt);
-  int recv_prev = 0;
-  int recv = __shfl_sync(FULL, (lane == 31) ? (int)(unsigned)e_cur[0] : cur[R - 1], (lane + 31) & 31);
 
+  int recv = 0, recv_prev = 0;
   for (int j = 0; j <= j_end; ++j) {
-    const int s0 = 4 * j;
+    const int s0 = C * j;
     __syncwarp();
-    if (j > 0) {
+    if (!fetch(s0)) {
+      if (!W.wait([&] { return fetch(s0); })) return;
+    }
+    if (lane == 31) sts_vol(cons_in, s0 + C);
+    int inv[C];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) e_cur[k] = e_nxt[k];
-      if (!valid(e_cur, s0)) {
-        // the prefetch ran ahead of the producer: wait, then repair what lane 0
-        // was sent for this chunk's first step
-        if (!W.wait([&] {
-              lds_u64x4(&ring_in[s0 & (RING - 1)], e_cur);
-              return valid(e_cur, s0);
-            }))
-          return;
-        if (lane == 0) recv = (int)(unsigned)e_cur[0];
-      }
-      lds_u64x4(&ring_in[(s0 + 4) & (RING - 1)], e_nxt);
-    }
-    if (lane == 31) sts_vol(cons_in, s0 + 4);
-    const int inv[5] = {(int)(unsigned)e_cur[0], (int)(unsigned)e_cur[1], (int)(unsigned)e_cur[2],
-                        (int)(unsigned)e_cur[3], (int)(unsigned)e_nxt[0]};
-    const int4 q_now = nextq;
-    nextq = ldg4(P.a_pad + base + 4 * (j + 2));
+    for (int k = 0; k < C; ++k) inv[k] = (int)(unsigned)e[k];
+    if (lane == 0) recv = inv[0];  // the incoming row's column s0 (see steps_chunk)
+    // symbols entering the window for the next chunk
+    int4 nq[C / 4];
+#pragma unroll
+    for (int i = 0; i < C / 4; ++i) nq[i] = ldg4(P.a_pad + base + s0 + C + 4 * i);
 
-    int outq[4];
-    const bool steady = (s0 >= 32 * R) && (s0 + 3 <= N);
+    int outq[C];
+    const bool steady = (s0 >= 32 * R) && (s0 + C - 1 <= N);
     if (padwarp) {
-      steps4<KIND, R, true, true>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0, lane, N,
-                                  padmask, smax, sstep);
+      steps_chunk<KIND, R, true, true>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0, lane,
+                                       N, padmask, smax, sstep);
     } else if (steady) {
-      steps4<KIND, R, false, false>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0, lane, N,
-                                    padmask, smax, sstep);
+      steps_chunk<KIND, R, false, false>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0,
+                                         lane, N, padmask, smax, sstep);
     } else {
-      steps4<KIND, R, true, false>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0, lane, N,
-                                   padmask, smax, sstep);
+      steps_chunk<KIND, R, true, false>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0, lane,
+                                        N, padmask, smax, sstep);
     }
 
-    // outgoing row: columns 4jo..4jo+3, jo = j - 8R
+    // outgoing row: columns pos..pos+C-1, pos = s0 - 32R
     const int pos = s0 - 32 * R;
     if (pos >= 0) {
       if (last) {
         if (lane == 31) {
-          volatile unsigned long long *dp = gdst + pos;
-          const unsigned long long w0 = gtag | (unsigned)outq[0], w1 = gtag | (unsigned)outq[1];
-          const unsigned long long w2 = gtag | (unsigned)outq[2], w3 = gtag | (unsigned)outq[3];
-          asm volatile("st.volatile.global.v2.u64 [%0], {%1,%2};" :: "l"(dp), "l"(w0), "l"(w1) : "memory");
-          asm volatile("st.volatile.global.v2.u64 [%0+16], {%1,%2};" :: "l"(dp), "l"(w2), "l"(w3) : "memory");
+#pragma unroll
+          for (int k = 0; k < C; k += 2) {
+            volatile unsigned long long *dp = gdst + pos + k;
+            const unsigned long long w0 = gtag | (unsigned)outq[k], w1 = gtag | (unsigned)outq[k + 1];
+            asm volatile("st.volatile.global.v2.u64 [%0], {%1,%2};" :: "l"(dp), "l"(w0), "l"(w1) : "memory");
+          }
         }
       } else {
-        if (pos + 4 - RING > cons_seen) {
+        if (pos + C - RING > cons_seen) {
           if (!W.wait([&] {
                 cons_seen = __shfl_sync(FULL, lds_vol(cons_out), 0);
-                return cons_seen >= pos + 4 - RING;
+                return cons_seen >= pos + C - RING;
               }))
             return;
         }
         if (lane == 31) {
-          const unsigned long long e[4] = {entry(pos, outq[0]), entry(pos + 1, outq[1]),
-                                           entry(pos + 2, outq[2]), entry(pos + 3, outq[3])};
-          sts_u64x4(&ring_out[pos & (RING - 1)], e);
+#pragma unroll
+          for (int k = 0; k < C; k += 4) {
+            const unsigned long long t[4] = {entry(pos + k, outq[k]), entry(pos + k + 1, outq[k + 1]),
+                                             entry(pos + k + 2, outq[k + 2]),
+                                             entry(pos + k + 3, outq[k + 3])};
+            sts_u64x4(&ring_out[(pos + k) & (RING - 1)], t);
+          }
         }
       }
     }
-    // slide the symbol window by four columns
+    // slide the symbol window by C columns
 #pragma unroll
-    for (int k = 0; k < R; ++k) win[k] = win[k + 4];
-    win[R] = q_now.x; win[R + 1] = q_now.y; win[R + 2] = q_now.z; win[R + 3] = q_now.w;
+    for (int k = 0; k < R; ++k) win[k] = win[k + C];
+#pragma unroll
+    for (int i = 0; i < C / 4; ++i) {
+      win[R + 4 * i] = nq[i].x; win[R + 4 * i + 1] = nq[i].y;
+      win[R + 4 * i + 2] = nq[i].z; win[R + 4 * i + 3] = nq[i].w;
+    }
   }
 
   // every row now holds its value at column N (cells beyond N were held)
@@ -605,7 +608,8 @@ int plain_run(Workspace &ws, int kind, const int *d_a, long long n1, const int *
   const long long nbands = (n2 + H - 1) / H;
   if (grid <= 0 || grid > nbands) grid = (int)std::min<long long>(nbands, ws.sms);
   const int nslot = grid + 2;
-  const long long stride = ((n1 + 1 + 3) / 4) * 4 + 4;
+  // the last warp writes C-column groups: a group starting at column <= n1 ends at < stride
+  const long long stride = ((n1 + 1 + C - 1) / C) * C + C;
   const long long a_pad_len = PADL + n1 + PADR;
   const long long b_pad_len = nbands * H;
   int rc = ws.reserve(a_pad_len, b_pad_len, (long long)nslot * stride, grid);

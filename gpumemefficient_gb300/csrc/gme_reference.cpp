@@ -3,7 +3,7 @@
 #include <climits>
 #include <mutex>
 
-#include "../../include/gme_reference.h"
+#include "gme_reference.h"
 
 namespace {
 std::mutex g_mu;
