@@ -34,6 +34,7 @@
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
+#include <type_traits>
 
 #include "gme_common.cuh"
 #include "gme_internal.h"
@@ -74,13 +75,17 @@ struct PlainParams {
   unsigned long long timeout_ns;
 };
 
-// Rings carry 64-bit entries {tag = column + 1, value}: a consumer knows an entry
-// is the one it wants from the entry itself, so no fence or separate progress
-// flag sits between producer and consumer (an acquire/release pair per chunk
-// would also wait for the in-flight symbol prefetch).  Only the consumer's
-// position is published, for back-pressure.  Rings are zeroed when a band starts.
+// Shared-memory rings between the warps of a band: plain int32 values plus one
+// tag word per C-column chunk (chunk index + 1), written with st.release after
+// the chunk's values and read with ld.acquire before them.  The producer
+// releases right after it has consumed its own symbol prefetch and the consumer
+// acquires before issuing the next one, so no fence waits on a global load in
+// flight.  Only the consumer's position is published back, for back-pressure.
+// Tags are zeroed when a band starts.
+constexpr int C = 16;  // wavefront steps (columns) per ring transaction
 template <int NW> struct __align__(16) PlainSmem {
-  unsigned long long ring[NW + 1][RING];
+  int ring[NW + 1][RING];
+  int tag[NW + 1][RING / C];
   int cons[NW + 1];
   int band;
   int abort;
@@ -126,8 +131,6 @@ __device__ __forceinline__ int4 ldg4(const int *p) { return __ldg(reinterpret_ca
 // hold their value.  PADROWS: rows beyond n2 copy the row above, so the warp's
 // bottom row equals row n2.
 // ---------------------------------------------------------------------------
-constexpr int C = 16;  // wavefront steps per ring transaction
-
 template <int KIND, int R, bool CHECKED, bool PADROWS>
 __device__ __forceinline__ void steps_chunk(const Rec<KIND> &rec, int (&cur)[R], int (&prv)[R],
                                             int &recv, int &recv_prev, const int (&win)[R + C],
@@ -211,46 +214,34 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
     win[k] = q.x; win[k + 1] = q.y; win[k + 2] = q.z; win[k + 3] = q.w;
   }
 
-  const unsigned long long *ring_in = S.ring[warp];
-  unsigned long long *ring_out = S.ring[warp + 1];
+  const int *ring_in = S.ring[warp];
+  int *ring_out = S.ring[warp + 1];
+  int *tag_in = S.tag[warp], *tag_out = S.tag[warp + 1];
   int *cons_in = &S.cons[warp], *cons_out = &S.cons[warp + 1];
   unsigned long long *gdst = P.slots + (long long)(band % P.nslot) * P.slot_stride;
   const unsigned long long gtag = (unsigned long long)(P.tag0 + (unsigned)band) << 32;
   int cons_seen = 0;
-  // last chunk: its output covers column N (outputs lag the inputs by 32R columns)
-  const int j_end = (N + 32 * R) / C;
-
-  // Incoming row, chunk j = columns Cj..Cj+C-1, as tagged entries {column+1, value}.
-  // Lanes may read a ring word at different moments, so the decision taken on the
-  // entries is made warp-uniform (a lane leaving a wait alone would strand the
-  // others at the next full-warp shuffle).  Equal tags imply equal values.
-  unsigned long long e[C];
-  auto fetch = [&](int p0) {
-    bool ok = true;
-#pragma unroll
-    for (int k = 0; k < C; k += 4) {
-      unsigned long long t[4];
-      lds_u64x4(&ring_in[(p0 + k) & (RING - 1)], t);
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        e[k + i] = t[i];
-        if (p0 + k + i <= N && (unsigned)(t[i] >> 32) != (unsigned)(p0 + k + i + 1)) ok = false;
-      }
-    }
-    return __all_sync(FULL, ok);
-  };
-
   int recv = 0, recv_prev = 0;
-  for (int j = 0; j <= j_end; ++j) {
+
+  // One chunk: wait for the incoming row's columns s0..s0+C-1, C steps, hand the
+  // bottom row's columns s0-32R.. on, slide the symbol window.
+  auto chunk = [&](int j, auto checked, auto padrows) -> bool {
+    constexpr bool CK = decltype(checked)::value, PD = decltype(padrows)::value;
     const int s0 = C * j;
     __syncwarp();
-    if (!fetch(s0)) {
-      if (!W.wait([&] { return fetch(s0); })) return;
+    if (s0 <= N) {
+      // Lanes may read the tag at different moments; the decision is made
+      // warp-uniform so that no lane leaves the wait alone.
+      auto ready = [&] { return __all_sync(FULL, ld_acquire_cta(&tag_in[j & (RING / C - 1)]) == j + 1); };
+      if (!ready() && !W.wait(ready)) return false;
     }
-    if (lane == 31) sts_vol(cons_in, s0 + C);
     int inv[C];
 #pragma unroll
-    for (int k = 0; k < C; ++k) inv[k] = (int)(unsigned)e[k];
+    for (int k = 0; k < C; k += 4) {
+      const int4 q = *reinterpret_cast<const int4 *>(&ring_in[(s0 + k) & (RING - 1)]);
+      inv[k] = q.x; inv[k + 1] = q.y; inv[k + 2] = q.z; inv[k + 3] = q.w;
+    }
+    if (lane == 31) sts_vol(cons_in, s0 + C);
     if (lane == 0) recv = inv[0];  // the incoming row's column s0 (see steps_chunk)
     // symbols entering the window for the next chunk
     int4 nq[C / 4];
@@ -258,19 +249,17 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
     for (int i = 0; i < C / 4; ++i) nq[i] = ldg4(P.a_pad + base + s0 + C + 4 * i);
 
     int outq[C];
-    const bool steady = (s0 >= 32 * R) && (s0 + C - 1 <= N);
-    if (padwarp) {
-      steps_chunk<KIND, R, true, true>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0, lane,
-                                       N, padmask, smax, sstep);
-    } else if (steady) {
-      steps_chunk<KIND, R, false, false>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0,
-                                         lane, N, padmask, smax, sstep);
-    } else {
-      steps_chunk<KIND, R, true, false>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0, lane,
-                                        N, padmask, smax, sstep);
+    steps_chunk<KIND, R, CK, PD>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0, lane, N,
+                                 padmask, smax, sstep);
+    // slide the symbol window by C columns (completes the prefetch before any release)
+#pragma unroll
+    for (int k = 0; k < R; ++k) win[k] = win[k + C];
+#pragma unroll
+    for (int i = 0; i < C / 4; ++i) {
+      win[R + 4 * i] = nq[i].x; win[R + 4 * i + 1] = nq[i].y;
+      win[R + 4 * i + 2] = nq[i].z; win[R + 4 * i + 3] = nq[i].w;
     }
-
-    // outgoing row: columns pos..pos+C-1, pos = s0 - 32R
+    // outgoing row: columns pos..pos+C-1, pos = s0 - 32R (chunk jo = j - 2R)
     const int pos = s0 - 32 * R;
     if (pos >= 0) {
       if (last) {
@@ -288,27 +277,38 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
                 cons_seen = __shfl_sync(FULL, lds_vol(cons_out), 0);
                 return cons_seen >= pos + C - RING;
               }))
-            return;
+            return false;
         }
         if (lane == 31) {
 #pragma unroll
-          for (int k = 0; k < C; k += 4) {
-            const unsigned long long t[4] = {entry(pos + k, outq[k]), entry(pos + k + 1, outq[k + 1]),
-                                             entry(pos + k + 2, outq[k + 2]),
-                                             entry(pos + k + 3, outq[k + 3])};
-            sts_u64x4(&ring_out[(pos + k) & (RING - 1)], t);
-          }
+          for (int k = 0; k < C; k += 4)
+            *reinterpret_cast<int4 *>(&ring_out[(pos + k) & (RING - 1)]) =
+                make_int4(outq[k], outq[k + 1], outq[k + 2], outq[k + 3]);
+          st_release_cta(&tag_out[(pos / C) & (RING / C - 1)], pos / C + 1);
         }
       }
     }
-    // slide the symbol window by C columns
-#pragma unroll
-    for (int k = 0; k < R; ++k) win[k] = win[k + C];
-#pragma unroll
-    for (int i = 0; i < C / 4; ++i) {
-      win[R + 4 * i] = nq[i].x; win[R + 4 * i + 1] = nq[i].y;
-      win[R + 4 * i + 2] = nq[i].z; win[R + 4 * i + 3] = nq[i].w;
-    }
+    return true;
+  };
+
+  using T = std::true_type;
+  using F = std::false_type;
+  // last chunk: its output covers column N (outputs lag the inputs by 32R columns)
+  const int j_end = (N + 32 * R) / C;
+  if (padwarp) {
+    for (int j = 0; j <= j_end; ++j)
+      if (!chunk(j, T{}, T{})) return;
+  } else {
+    // steady chunks: every cell of the warp has 1 <= x <= N for all C steps
+    const int j_lo = min((32 * R) / C, j_end + 1);
+    const int j_hi = max(min((N - C + 1) / C, j_end), j_lo - 1);
+    int j = 0;
+    for (; j < j_lo; ++j)
+      if (!chunk(j, T{}, F{})) return;
+    for (; j <= j_hi; ++j)
+      if (!chunk(j, F{}, F{})) return;
+    for (; j <= j_end; ++j)
+      if (!chunk(j, T{}, F{})) return;
   }
 
   // every row now holds its value at column N (cells beyond N were held)
@@ -335,7 +335,7 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int la
   const unsigned long long *src =
       band > 0 ? P.slots + (long long)((band - 1) % P.nslot) * P.slot_stride : nullptr;
   const unsigned src_tag = P.tag0 + (unsigned)(band - 1);
-  unsigned long long *ring0 = S.ring[0];
+  int *ring0 = S.ring[0];
   int in_pos = 0;
   unsigned idle = 0;
   unsigned long long deadline = 0;
@@ -371,11 +371,13 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int la
       const int lanes_ok = (okm == FULL) ? 32 : (__ffs(~okm) - 1);
       const int n = min(4 * lanes_ok, want);
       if (n > 0) {
-        if (4 * lane < n) {
-          const unsigned long long e[4] = {entry(p, v[0]), entry(p + 1, v[1]), entry(p + 2, v[2]),
-                                           entry(p + 3, v[3])};
-          sts_u64x4(&ring0[p & (RING - 1)], e);
-        }
+        if (4 * lane < n)
+          *reinterpret_cast<int4 *>(&ring0[p & (RING - 1)]) = make_int4(v[0], v[1], v[2], v[3]);
+        __syncwarp();
+        // release the chunks this round completed (the last one may be partial)
+        const int c0 = in_pos / C;
+        const int c1 = (in_pos + n >= N1) ? (N1 + C - 1) / C : (in_pos + n) / C;
+        if (lane < c1 - c0) st_release_cta(&S.tag[0][(c0 + lane) & (RING / C - 1)], c0 + lane + 1);
         in_pos += n;
         moved = true;
       }
@@ -417,7 +419,7 @@ __global__ void __launch_bounds__((NW + 1) * 32, 1) plain_kernel(PlainParams P) 
 #pragma unroll
       for (int k = 0; k <= NW; ++k) S.cons[k] = 0;
     }
-    for (int i = threadIdx.x; i < (NW + 1) * RING; i += blockDim.x) (&S.ring[0][0])[i] = 0ull;
+    for (int i = threadIdx.x; i < (NW + 1) * (RING / C); i += blockDim.x) (&S.tag[0][0])[i] = 0;
     __syncthreads();
     const int band = S.band;
     if (band >= P.nbands) break;
