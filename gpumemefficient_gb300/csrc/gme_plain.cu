@@ -127,25 +127,41 @@ __device__ __forceinline__ int4 ldg4(const int *p) { return __ldg(reinterpret_ca
 // the bottom row is computed next and shuffled to the lane below at once, and
 // the other rows are computed while the shuffle is in flight.
 //
+// Symbols: a circular window of 2C registers; symbol i (relative to the lane's
+// base, column x = i - r + 1 for row r) lives at win[i mod 2C].  Chunk j reads
+// i in [Cj-R+1, Cj+C-1] and, at step R (after the last read of the previous
+// chunk's tail), loads the next chunk's C symbols into the other half.  PAR is
+// j & 1, so every index is a compile-time constant and nothing is shifted.
+//
 // CHECKED: some cells of the warp fall outside 1 <= x <= n1 (ramp-in/out) and
 // hold their value.  PADROWS: rows beyond n2 copy the row above, so the warp's
 // bottom row equals row n2.
 // ---------------------------------------------------------------------------
-template <int KIND, int R, bool CHECKED, bool PADROWS>
+template <int KIND, int R, int PAR, bool CHECKED, bool PADROWS>
 __device__ __forceinline__ void steps_chunk(const Rec<KIND> &rec, int (&cur)[R], int (&prv)[R],
-                                            int &recv, int &recv_prev, const int (&win)[R + C],
-                                            const int (&bs)[R], const int (&inv)[C], int (&outq)[C],
-                                            int s0, int lane, int N, unsigned padmask,
-                                            int (&smax)[R], int (&sstep)[R]) {
+                                            int &recv, int &recv_prev, int (&win)[2 * C],
+                                            const int *sym_next, const int (&bs)[R],
+                                            const int (&inv)[C], int (&outq)[C], int s0, int lane,
+                                            int N, unsigned padmask, int (&smax)[R], int (&sstep)[R]) {
+  static_assert(R < C, "the window refill at step R needs R < C");
 #pragma unroll
   for (int q = 0; q < C; ++q) {
+    if (q == R) {
+#pragma unroll
+      for (int i = 0; i < C / 4; ++i) {
+        const int4 v = ldg4(sym_next + 4 * i);
+        const int h = (PAR ^ 1) * C + 4 * i;
+        win[h] = v.x; win[h + 1] = v.y; win[h + 2] = v.z; win[h + 3] = v.w;
+      }
+    }
     const int s = s0 + q;
     const int rcv = recv;  // the cell above row 0 for this step
     outq[q] = cur[R - 1];  // lane 31: bottom cell after step s-1 (column s-32R)
     int D[R];
 #pragma unroll
     for (int r = 0; r < R; ++r)
-      D[r] = (r ? prv[r - 1] : recv_prev) + (win[R + q - r] == bs[r] ? rec.ceq : rec.cne);
+      D[r] = (r ? prv[r - 1] : recv_prev) +
+             (win[(PAR * C + q - r + 2 * C) % (2 * C)] == bs[r] ? rec.ceq : rec.cne);
     int nv[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -166,7 +182,7 @@ __device__ __forceinline__ void steps_chunk(const Rec<KIND> &rec, int (&cur)[R],
       if (k == 0) {
         // lane 31 feeds the incoming row to lane 0 through the same shuffle; the
         // chunk's last step sends nothing useful: lane 0 re-latches the next
-        // chunk's first column from the validated ring entries
+        // chunk's first column from the validated ring values
         const int send = (lane == 31) ? inv[q + 1 < C ? q + 1 : C - 1] : v;
         recv = __shfl_sync(FULL, send, (lane + 31) & 31);  // for step s+1
         recv_prev = rcv;
@@ -177,12 +193,17 @@ __device__ __forceinline__ void steps_chunk(const Rec<KIND> &rec, int (&cur)[R],
   }
 }
 
-// One compute warp sweeping its 32*R rows of a band across all N columns.
-// Warps hand their bottom row to the next warp through a shared ring; the last
-// active warp of the band writes it straight to the band's global slot.
+// One compute warp sweeping its 32*R rows of a band across all N columns.  Every
+// warp hands its bottom row to the next ring (the last active warp's ring is
+// drained to global memory by the band's I/O warp).
+//
+// The incoming row runs one chunk ahead: during chunk j the warp already reads
+// the tag and values of chunk j+1, so at the start of chunk j+1 the check is a
+// register compare.  In steady state this makes each warp trail the one above
+// by one extra chunk (C steps), which buys the latency of the shared loads.
 template <int KIND, int R, int NW>
 __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, int warp, int lane,
-                             int active, Waiter &W, SwBest &tb) {
+                             Waiter &W, SwBest &tb) {
   const Rec<KIND> rec(P.sc);
   const int N = P.N, M = P.M;
   const int yl = band * P.H + warp * 32 * R + lane * R + 1;  // first row of this lane
@@ -202,90 +223,83 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
     if (yl + r > M) padmask |= 1u << r;
   }
   const bool padwarp = __any_sync(FULL, padmask != 0);
-  const bool last = (warp == active - 1);
 
-  // Symbol window: win[k] = a_pad[base + s0 - R + k]; the symbol of row r at
-  // step s0+q is win[R+q-r] (column x = s0+q - lane*R - r, a[x-1]).
-  const long long base = PADL - 1 - lane * R;
-  int win[R + C];
+  // Symbol window for chunk 0: i in [0, C) at win[0..C), i in [-R, 0) at win[2C-R..2C).
+  const int *sym = P.a_pad + (PADL - 1 - lane * R);  // sym[i]: symbol index i of this lane
+  int win[2 * C];
 #pragma unroll
-  for (int k = 0; k < R + C; k += 4) {
-    int4 q = ldg4(P.a_pad + base - R + k);
+  for (int k = 0; k < C; k += 4) {
+    const int4 q = ldg4(sym + k);
     win[k] = q.x; win[k + 1] = q.y; win[k + 2] = q.z; win[k + 3] = q.w;
   }
+#pragma unroll
+  for (int k = 0; k < R; k += 4) {
+    const int4 q = ldg4(sym - R + k);
+    win[2 * C - R + k] = q.x; win[2 * C - R + k + 1] = q.y;
+    win[2 * C - R + k + 2] = q.z; win[2 * C - R + k + 3] = q.w;
+  }
+#pragma unroll
+  for (int k = C; k < 2 * C - R; ++k) win[k] = 0;
 
   const int *ring_in = S.ring[warp];
   int *ring_out = S.ring[warp + 1];
   int *tag_in = S.tag[warp], *tag_out = S.tag[warp + 1];
   int *cons_in = &S.cons[warp], *cons_out = &S.cons[warp + 1];
-  unsigned long long *gdst = P.slots + (long long)(band % P.nslot) * P.slot_stride;
-  const unsigned long long gtag = (unsigned long long)(P.tag0 + (unsigned)band) << 32;
   int cons_seen = 0;
   int recv = 0, recv_prev = 0;
 
-  // One chunk: wait for the incoming row's columns s0..s0+C-1, C steps, hand the
-  // bottom row's columns s0-32R.. on, slide the symbol window.
-  auto chunk = [&](int j, auto checked, auto padrows) -> bool {
-    constexpr bool CK = decltype(checked)::value, PD = decltype(padrows)::value;
-    const int s0 = C * j;
-    __syncwarp();
-    if (s0 <= N) {
-      // Lanes may read the tag at different moments; the decision is made
-      // warp-uniform so that no lane leaves the wait alone.
-      auto ready = [&] { return __all_sync(FULL, ld_acquire_cta(&tag_in[j & (RING / C - 1)]) == j + 1); };
-      if (!ready() && !W.wait(ready)) return false;
-    }
-    int inv[C];
+  // incoming-row buffers by chunk parity: ib[PAR] holds chunk j, ib[PAR^1] chunk j+1
+  int ib[2][C];
+  int tag_next;
+  auto load_in = [&](int j, int (&dst)[C]) {
 #pragma unroll
     for (int k = 0; k < C; k += 4) {
-      const int4 q = *reinterpret_cast<const int4 *>(&ring_in[(s0 + k) & (RING - 1)]);
-      inv[k] = q.x; inv[k + 1] = q.y; inv[k + 2] = q.z; inv[k + 3] = q.w;
+      const int4 q = *reinterpret_cast<const int4 *>(&ring_in[(C * j + k) & (RING - 1)]);
+      dst[k] = q.x; dst[k + 1] = q.y; dst[k + 2] = q.z; dst[k + 3] = q.w;
+    }
+  };
+  tag_next = ld_acquire_cta(&tag_in[0]);
+  load_in(0, ib[0]);
+
+  auto chunk = [&](int j, auto par, auto checked, auto padrows) -> bool {
+    constexpr int PAR = decltype(par)::value;
+    constexpr bool CK = decltype(checked)::value, PD = decltype(padrows)::value;
+    int(&inv)[C] = ib[PAR];
+    const int s0 = C * j;
+    __syncwarp();
+    if (s0 <= N && !__all_sync(FULL, tag_next == j + 1)) {
+      // the read-ahead found the chunk not yet written: wait for it, then reread.
+      // Lanes may read the tag at different moments; the decision is warp-uniform
+      // so that no lane leaves the wait alone.
+      auto ready = [&] { return __all_sync(FULL, ld_acquire_cta(&tag_in[j & (RING / C - 1)]) == j + 1); };
+      if (!W.wait(ready)) return false;
+      load_in(j, inv);
     }
     if (lane == 31) sts_vol(cons_in, s0 + C);
     if (lane == 0) recv = inv[0];  // the incoming row's column s0 (see steps_chunk)
-    // symbols entering the window for the next chunk
-    int4 nq[C / 4];
-#pragma unroll
-    for (int i = 0; i < C / 4; ++i) nq[i] = ldg4(P.a_pad + base + s0 + C + 4 * i);
+    // read ahead: chunk j+1
+    tag_next = ld_acquire_cta(&tag_in[(j + 1) & (RING / C - 1)]);
+    load_in(j + 1, ib[PAR ^ 1]);
 
     int outq[C];
-    steps_chunk<KIND, R, CK, PD>(rec, cur, prv, recv, recv_prev, win, bs, inv, outq, s0, lane, N,
-                                 padmask, smax, sstep);
-    // slide the symbol window by C columns (completes the prefetch before any release)
-#pragma unroll
-    for (int k = 0; k < R; ++k) win[k] = win[k + C];
-#pragma unroll
-    for (int i = 0; i < C / 4; ++i) {
-      win[R + 4 * i] = nq[i].x; win[R + 4 * i + 1] = nq[i].y;
-      win[R + 4 * i + 2] = nq[i].z; win[R + 4 * i + 3] = nq[i].w;
-    }
-    // outgoing row: columns pos..pos+C-1, pos = s0 - 32R (chunk jo = j - 2R)
+    steps_chunk<KIND, R, PAR, CK, PD>(rec, cur, prv, recv, recv_prev, win, sym + s0 + C, bs, inv,
+                                      outq, s0, lane, N, padmask, smax, sstep);
+    // outgoing row: columns pos..pos+C-1, pos = s0 - 32R (chunk j - 2R)
     const int pos = s0 - 32 * R;
     if (pos >= 0) {
-      if (last) {
-        if (lane == 31) {
+      if (pos + C - RING > cons_seen) {
+        if (!W.wait([&] {
+              cons_seen = __shfl_sync(FULL, lds_vol(cons_out), 0);
+              return cons_seen >= pos + C - RING;
+            }))
+          return false;
+      }
+      if (lane == 31) {
 #pragma unroll
-          for (int k = 0; k < C; k += 2) {
-            volatile unsigned long long *dp = gdst + pos + k;
-            const unsigned long long w0 = gtag | (unsigned)outq[k], w1 = gtag | (unsigned)outq[k + 1];
-            asm volatile("st.volatile.global.v2.u64 [%0], {%1,%2};" :: "l"(dp), "l"(w0), "l"(w1) : "memory");
-          }
-        }
-      } else {
-        if (pos + C - RING > cons_seen) {
-          if (!W.wait([&] {
-                cons_seen = __shfl_sync(FULL, lds_vol(cons_out), 0);
-                return cons_seen >= pos + C - RING;
-              }))
-            return false;
-        }
-        if (lane == 31) {
-#pragma unroll
-          for (int k = 0; k < C; k += 4)
-            *reinterpret_cast<int4 *>(&ring_out[(pos + k) & (RING - 1)]) =
-                make_int4(outq[k], outq[k + 1], outq[k + 2], outq[k + 3]);
-          st_release_cta(&tag_out[(pos / C) & (RING / C - 1)], pos / C + 1);
-        }
+        for (int k = 0; k < C; k += 4)
+          *reinterpret_cast<int4 *>(&ring_out[(pos + k) & (RING - 1)]) =
+              make_int4(outq[k], outq[k + 1], outq[k + 2], outq[k + 3]);
+        st_release_cta(&tag_out[(pos / C) & (RING / C - 1)], pos / C + 1);
       }
     }
     return true;
@@ -293,22 +307,33 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
 
   using T = std::true_type;
   using F = std::false_type;
+  using P0 = std::integral_constant<int, 0>;
+  using P1 = std::integral_constant<int, 1>;
+  // chunks ja..jb (inclusive) in parity order
+  auto range = [&](int ja, int jb, auto ck, auto pd) -> bool {
+    int j = ja;
+    if (j <= jb && (j & 1)) {
+      if (!chunk(j, P1{}, ck, pd)) return false;
+      ++j;
+    }
+    for (; j + 1 <= jb; j += 2) {
+      if (!chunk(j, P0{}, ck, pd)) return false;
+      if (!chunk(j + 1, P1{}, ck, pd)) return false;
+    }
+    if (j <= jb && !chunk(j, P0{}, ck, pd)) return false;
+    return true;
+  };
   // last chunk: its output covers column N (outputs lag the inputs by 32R columns)
   const int j_end = (N + 32 * R) / C;
   if (padwarp) {
-    for (int j = 0; j <= j_end; ++j)
-      if (!chunk(j, T{}, T{})) return;
+    if (!range(0, j_end, T{}, T{})) return;
   } else {
     // steady chunks: every cell of the warp has 1 <= x <= N for all C steps
     const int j_lo = min((32 * R) / C, j_end + 1);
     const int j_hi = max(min((N - C + 1) / C, j_end), j_lo - 1);
-    int j = 0;
-    for (; j < j_lo; ++j)
-      if (!chunk(j, T{}, F{})) return;
-    for (; j <= j_hi; ++j)
-      if (!chunk(j, F{}, F{})) return;
-    for (; j <= j_end; ++j)
-      if (!chunk(j, T{}, F{})) return;
+    if (!range(0, j_lo - 1, T{}, F{})) return;
+    if (!range(j_lo, j_hi, F{}, F{})) return;
+    if (!range(j_hi + 1, j_end, T{}, F{})) return;
   }
 
   // every row now holds its value at column N (cells beyond N were held)
@@ -325,47 +350,77 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
   }
 }
 
-// The I/O warp of a band: forwards the band's incoming row into ring 0, each
-// lane moving four consecutive columns per round.  Band 0 reads the table's top
-// border; later bands poll the tagged words of the band above (one L2 round
-// trip per poll, no flag).
+// The I/O warp of a band.  Incoming row: forwards the band above's tagged global
+// words (or, for band 0, the table's top border) into ring 0 and releases each
+// completed chunk.  Outgoing row: copies the chunks the last compute warp has
+// released from ring `active` to the band's global slot as tagged words.  The
+// global poll is issued first and consumed last, so its L2 round trip overlaps
+// the drain.
 template <int KIND, int NW>
-__device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int lane) {
+__device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int active, int lane) {
   const int N1 = P.N + 1;
   const unsigned long long *src =
       band > 0 ? P.slots + (long long)((band - 1) % P.nslot) * P.slot_stride : nullptr;
+  unsigned long long *dst = P.slots + (long long)(band % P.nslot) * P.slot_stride;
   const unsigned src_tag = P.tag0 + (unsigned)(band - 1);
+  const unsigned long long dst_tag = (unsigned long long)(P.tag0 + (unsigned)band) << 32;
   int *ring0 = S.ring[0];
-  int in_pos = 0;
+  const int *ringo = S.ring[active];
+  const int *tago = S.tag[active];
+  int in_pos = 0, out_pos = 0;
   unsigned idle = 0;
   unsigned long long deadline = 0;
 
-  while (in_pos < N1) {
+  while (in_pos < N1 || out_pos < N1) {
     bool moved = false;
+    // (a) incoming: issue the poll of up to 128 columns (consumed in (c))
     const int space = RING - (in_pos - __shfl_sync(FULL, lds_vol(&S.cons[0]), 0));
-    const int want = min(N1 - in_pos, space);
-    if (want > 0) {
-      const int p = in_pos + 4 * lane;
-      int v[4] = {0, 0, 0, 0};
-      bool ok = true;
-      if (4 * lane < want) {
-        if (band == 0) {
+    const int want = in_pos < N1 ? min(N1 - in_pos, space) : 0;
+    const int p = in_pos + 4 * lane;
+    unsigned long long w[4] = {0, 0, 0, 0};
+    if (want > 0 && band > 0 && 4 * lane < want) {
+      const volatile unsigned long long *sp = src + p;
+      asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2];" : "=l"(w[0]), "=l"(w[1]) : "l"(sp));
+      asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2+16];" : "=l"(w[2]), "=l"(w[3]) : "l"(sp));
+    }
+    // (b) outgoing: lane k looks at chunk out_pos/C + k
+    if (out_pos < N1) {
+      const int c = out_pos / C + lane;
+      bool ready = false;
+      if (lane < 8 && c * C < N1) ready = ld_acquire_cta(&tago[c & (RING / C - 1)]) == c + 1;
+      const unsigned rm = __ballot_sync(FULL, ready);
+      const int nch = (rm == FULL) ? 32 : (__ffs(~rm) - 1);
+      if (nch > 0) {
+        if (lane < nch) {
 #pragma unroll
-          for (int k = 0; k < 4; ++k) v[k] = Rec<KIND>::top(p + k, P.sc.ed_rule);
-        } else {
-          const volatile unsigned long long *sp = src + p;
-          unsigned long long w0, w1, w2, w3;
-          asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2];" : "=l"(w0), "=l"(w1) : "l"(sp));
-          asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2+16];" : "=l"(w2), "=l"(w3) : "l"(sp));
-          const unsigned long long w[4] = {w0, w1, w2, w3};
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            v[k] = (int)(unsigned)w[k];
-            if (p + k < N1 && (unsigned)(w[k] >> 32) != src_tag) ok = false;
+          for (int k = 0; k < C; k += 4) {
+            const int4 q = *reinterpret_cast<const int4 *>(&ringo[(c * C + k) & (RING - 1)]);
+            volatile unsigned long long *dp = dst + c * C + k;
+            const unsigned long long w0 = dst_tag | (unsigned)q.x, w1 = dst_tag | (unsigned)q.y;
+            const unsigned long long w2 = dst_tag | (unsigned)q.z, w3 = dst_tag | (unsigned)q.w;
+            asm volatile("st.volatile.global.v2.u64 [%0], {%1,%2};" :: "l"(dp), "l"(w0), "l"(w1) : "memory");
+            asm volatile("st.volatile.global.v2.u64 [%0+16], {%1,%2};" :: "l"(dp), "l"(w2), "l"(w3) : "memory");
           }
         }
+        out_pos = min(out_pos + nch * C, N1);
+        __syncwarp();
+        if (lane == 0) sts_vol(&S.cons[active], out_pos);
+        moved = true;
+      }
+    }
+    // (c) incoming: take the valid prefix of the poll and release completed chunks
+    if (want > 0) {
+      int v[4];
+      bool ok = 4 * lane < want;
+      if (band == 0) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] = Rec<KIND>::top(p + k, P.sc.ed_rule);
       } else {
-        ok = false;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          v[k] = (int)(unsigned)w[k];
+          if (p + k < N1 && (unsigned)(w[k] >> 32) != src_tag) ok = false;
+        }
       }
       const unsigned okm = __ballot_sync(FULL, ok);
       const int lanes_ok = (okm == FULL) ? 32 : (__ffs(~okm) - 1);
@@ -389,7 +444,7 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int la
       if (idle == 0) deadline = globaltimer_ns() + P.timeout_ns;
       if ((++idle & 15u) == 0) {
         int give = 0;
-        if (S.abort) give = 1;
+        if (*(volatile int *)&S.abort) give = 1;
         else if (ld_relaxed_gpu_s32(&P.ctrl[1]) != 0) give = 2;
         else if (globaltimer_ns() > deadline) give = 3;
         give = __shfl_sync(FULL, give, 0);
@@ -399,8 +454,7 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int la
           return;
         }
       }
-      // a full ring waits on the compute warps; an empty poll already cost an L2 round trip
-      if (want <= 0) __nanosleep(256);
+      if (band == 0 || in_pos >= N1) __nanosleep(128);
     }
   }
 }
@@ -426,9 +480,9 @@ __global__ void __launch_bounds__((NW + 1) * 32, 1) plain_kernel(PlainParams P) 
     const int rows_left = P.M - band * P.H;
     const int active = min(NW, (rows_left + 32 * R - 1) / (32 * R));
     if (warp < NW) {
-      if (warp < active) compute_band<KIND, R, NW>(P, S, band, warp, lane, active, W, tb);
+      if (warp < active) compute_band<KIND, R, NW>(P, S, band, warp, lane, W, tb);
     } else {
-      io_band<KIND, NW>(P, S, band, lane);
+      io_band<KIND, NW>(P, S, band, active, lane);
     }
     __syncthreads();
   }
