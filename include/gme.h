@@ -114,6 +114,25 @@ gme_status gme_align_device(gme_context *ctx, gme_kind kind, const int32_t *d_a,
                             gme_result *d_out, int32_t *d_last_row, int32_t *d_last_col,
                             void *stream);
 
+/* ---- plain path without allocation --------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc (code
+ * running inside another runtime's memory pool, a plugin that must not allocate on
+ * its hot path, a loop whose allocator is fenced off): the same computation as
+ * gme_align_device, with every byte of scratch taken from one static device array
+ * of about 4.4 MB that each GPU loading the library holds until exit.  Needs no
+ * context and allocates nothing; runs on the calling thread's current device,
+ * asynchronously on `stream`.
+ *   - Sequences longer than GME_NOALLOC_MAX_LEN are rejected with GME_ERR_INVALID.
+ *   - The first call on a device resolves the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - All calls on a device share the array: calls that overlap on the GPU (other
+ *     streams, other host threads) race and must be serialised by the caller. */
+#define GME_NOALLOC_MAX_LEN 8192
+gme_status gme_align_device_noalloc(gme_kind kind, const int32_t *d_a, int64_t n1,
+                                    const int32_t *d_b, int64_t n2, const gme_scoring *sc,
+                                    gme_result *d_out, int32_t *d_last_row, int32_t *d_last_col,
+                                    void *stream);
+
 /* ---- diagnostics ------------------------------------------------------------- */
 /* Runs the bounded device wait on a flag that nothing sets and reports what the
  * kernel returned (expected GME_ERR_TIMEOUT after `timeout_ns`).  Tests use it to
