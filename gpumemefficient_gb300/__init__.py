@@ -49,6 +49,22 @@ class Result(ctypes.Structure):
                 ("status", ctypes.c_int32), ("kind", ctypes.c_int32)]
 
 
+class Pair(ctypes.Structure):
+    _fields_ = [("a_off", ctypes.c_int64), ("b_off", ctypes.c_int64), ("n1", ctypes.c_int32),
+                ("n2", ctypes.c_int32), ("kind", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class BatchConfig(ctypes.Structure):
+    _fields_ = [("warps_per_block", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
+                ("warp_max_rows", ctypes.c_int32), ("warp_max_cols", ctypes.c_int32)]
+
+
+PAIR_DTYPE = np.dtype([("a_off", "<i8"), ("b_off", "<i8"), ("n1", "<i4"), ("n2", "<i4"),
+                       ("kind", "<i4"), ("reserved", "<i4")])
+RESULT_DTYPE = np.dtype([("score", "<i4"), ("sw_max", "<i4"), ("sw_max_y", "<i8"),
+                         ("sw_max_x", "<i8"), ("status", "<i4"), ("kind", "<i4")])
+
+
 class PlainConfig(ctypes.Structure):
     _fields_ = [("rows_per_lane", ctypes.c_int32), ("warps_per_band", ctypes.c_int32),
                 ("grid", ctypes.c_int32), ("reserved", ctypes.c_int32)]
@@ -75,6 +91,12 @@ def _declare(L):
                             c.POINTER(Result), _vp, _vp]
     L.gme_align_device.argtypes = [_vp, c.c_int, _vp, c.c_int64, _vp, c.c_int64,
                                    c.POINTER(Scoring), _vp, _vp, _vp, _vp]
+    L.gme_set_batch_config.argtypes = [_vp, c.POINTER(BatchConfig)]
+    L.gme_align_batch.argtypes = [_vp, _vp, c.c_int64, _vp, c.c_int64, c.POINTER(Scoring), _vp]
+    L.gme_align_batch_device.argtypes = [_vp, _vp, c.c_int64, _vp, c.c_int64, c.POINTER(Scoring),
+                                         _vp, _vp]
+    L.gme_batch_stats.argtypes = [_vp, c.POINTER(c.c_int64), c.POINTER(c.c_int64),
+                                  c.POINTER(c.c_int64)]
     L.gme_debug_wait_timeout.argtypes = [_vp, c.c_uint64, c.POINTER(c.c_int32)]
     L.gme_launch_count.argtypes = [_vp]
     L.gme_launch_count.restype = c.c_int64
@@ -187,11 +209,54 @@ class Context:
                                       d_out, d_last_row or None, d_last_col or None,
                                       stream or None), self.handle)
 
+    def set_batch_config(self, warps_per_block: int = 0, blocks_per_sm: int = 0,
+                         warp_max_rows: int = 0, warp_max_cols: int = 0):
+        cfg = BatchConfig(warps_per_block, blocks_per_sm, warp_max_rows, warp_max_cols)
+        _check(lib().gme_set_batch_config(self.handle, ctypes.byref(cfg)), self.handle)
+
+    def batch_stats(self) -> dict:
+        b, w, l = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().gme_batch_stats(self.handle, ctypes.byref(b), ctypes.byref(w), ctypes.byref(l)))
+        return {"block_jobs": b.value, "warp_jobs": w.value, "long_jobs": l.value}
+
+    def align_batch(self, kinds, seqs_a, seqs_b, sc: Optional[Scoring] = None) -> np.ndarray:
+        """Many alignments in one launch; returns a structured array of results."""
+        symbols, pairs = pack_batch(kinds, seqs_a, seqs_b)
+        res = np.zeros(len(pairs), RESULT_DTYPE)
+        sc = sc or scoring()
+        _check(lib().gme_align_batch(self.handle, symbols.ctypes.data, len(symbols),
+                                     pairs.ctypes.data, len(pairs), ctypes.byref(sc),
+                                     res.ctypes.data), self.handle)
+        return res
+
+    def align_batch_device(self, d_symbols: int, nsym: int, pairs: np.ndarray, d_results: int,
+                           sc: Optional[Scoring] = None, stream: int = 0):
+        """Device symbols/results, host pair list (a PAIR_DTYPE array); asynchronous."""
+        pairs = np.ascontiguousarray(pairs, PAIR_DTYPE)
+        sc = sc or scoring()
+        _check(lib().gme_align_batch_device(self.handle, d_symbols, nsym, pairs.ctypes.data,
+                                            len(pairs), ctypes.byref(sc), d_results,
+                                            stream or None), self.handle)
+
     def debug_wait_timeout(self, timeout_ns: int) -> int:
         """Runs a bounded device wait on a flag nothing sets; returns the kernel's status."""
         ks = ctypes.c_int32(-1)
         _check(lib().gme_debug_wait_timeout(self.handle, timeout_ns, ctypes.byref(ks)), self.handle)
         return int(ks.value)
+
+
+def pack_batch(kinds, seqs_a, seqs_b):
+    """One int32 symbol buffer plus a PAIR_DTYPE pair list for the batched entry points."""
+    parts, pairs = [], np.zeros(len(kinds), PAIR_DTYPE)
+    off = 0
+    for i, (k, a, b) in enumerate(zip(kinds, seqs_a, seqs_b)):
+        a = np.asarray(a, np.int32)
+        b = np.asarray(b, np.int32)
+        pairs[i] = (off, off + len(a), len(a), len(b), int(k), 0)
+        parts += [a, b]
+        off += len(a) + len(b)
+    symbols = np.ascontiguousarray(np.concatenate(parts) if parts else np.zeros(1, np.int32), np.int32)
+    return symbols, pairs
 
 
 _default_ctx: Optional[Context] = None

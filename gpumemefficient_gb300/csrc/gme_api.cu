@@ -70,6 +70,38 @@ void Workspace::release() {
   a_pad_cap = b_pad_cap = slots_cap = 0; best_cap = 0;
 }
 
+static int grow_ll(void **p, long long *cap, long long need, size_t elem, Workspace &ws, const char *what) {
+  return grow(p, cap, need, elem, ws, what, false);
+}
+
+int BatchArena::reserve(long long staged, long long nseg, long long njobs, Workspace &ws) {
+  int rc;
+  if ((rc = grow_ll((void **)&d_staged, &staged_cap, staged, sizeof(int), ws, "cudaMalloc(batch staged)"))) return rc;
+  if (seg_cap < nseg || !d_from) {
+    long long c0 = seg_cap, c1 = seg_cap, c2 = seg_cap, c3 = seg_cap, c4 = seg_cap;
+    if ((rc = grow_ll((void **)&d_from, &c0, nseg, 8, ws, "cudaMalloc(batch from)")) ||
+        (rc = grow_ll((void **)&d_to, &c1, nseg, 8, ws, "cudaMalloc(batch to)")) ||
+        (rc = grow_ll((void **)&d_len, &c2, nseg, 4, ws, "cudaMalloc(batch len)")) ||
+        (rc = grow_ll((void **)&d_padl, &c3, nseg, 4, ws, "cudaMalloc(batch padl)")) ||
+        (rc = grow_ll((void **)&d_total, &c4, nseg, 4, ws, "cudaMalloc(batch total)")))
+      return rc;
+    seg_cap = std::min(std::min(c0, c1), std::min(std::min(c2, c3), c4));
+  }
+  if ((rc = grow_ll((void **)&d_jobs, &jobs_cap, njobs, sizeof(BatchJob), ws, "cudaMalloc(batch jobs)"))) return rc;
+  if (!d_ctrl) {
+    cudaError_t e = cudaMalloc(&d_ctrl, 16 * sizeof(int));
+    if (e != cudaSuccess) return ws.fail(e, "cudaMalloc(batch ctrl)");
+  }
+  return ST_OK;
+}
+
+void BatchArena::release() {
+  cudaFree(d_staged); cudaFree(d_from); cudaFree(d_to); cudaFree(d_len); cudaFree(d_padl);
+  cudaFree(d_total); cudaFree(d_jobs); cudaFree(d_ctrl);
+  d_staged = nullptr; d_from = d_to = nullptr; d_len = d_padl = d_total = nullptr; d_jobs = nullptr;
+  d_ctrl = nullptr; staged_cap = seg_cap = jobs_cap = 0;
+}
+
 // A kernel that waits, with the library's bounded wait, on a word nothing sets.
 __global__ void debug_wait_kernel(int *ctrl, const int *never, unsigned long long timeout_ns) {
   __shared__ int abort_flag;
@@ -112,6 +144,11 @@ struct gme_context {
   int *d_col = nullptr; long long d_col_cap = 0;
   gme_result *d_res = nullptr;
   gme_result *h_res = nullptr;  // pinned
+  // batched path
+  gme::BatchArena batch;
+  gme::BatchTuning batch_tune;
+  int *d_bsym = nullptr; long long d_bsym_cap = 0;
+  gme_result *d_bres = nullptr; long long d_bres_cap = 0;
 };
 
 using gme::ST_OK;
@@ -237,6 +274,8 @@ gme_status gme_destroy(gme_context *ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   ctx->ws.release();
+  ctx->batch.release();
+  cudaFree(ctx->d_bsym); cudaFree(ctx->d_bres);
   cudaFree(ctx->d_a); cudaFree(ctx->d_b); cudaFree(ctx->d_row); cudaFree(ctx->d_col);
   cudaFree(ctx->d_res);
   cudaFreeHost(ctx->h_res);
@@ -260,7 +299,7 @@ gme_status gme_set_plain_config(gme_context *ctx, const gme_plain_config *cfg) {
   if (!cfg) { ctx->cfg = gme_plain_config{}; return GME_OK; }
   if ((cfg->rows_per_lane || cfg->warps_per_band) &&
       !gme::plain_config_valid(cfg->rows_per_lane, cfg->warps_per_band)) {
-    ctx->ws.last_error = "plain config: rows_per_lane 4 with warps_per_band 1,2,3,4,6,8, or rows_per_lane 8 with 1..4";
+    ctx->ws.last_error = "plain config: rows_per_lane must be 4, warps_per_band 1, 2, 3, 4, 6 or 8";
     return GME_ERR_INVALID;
   }
   if (cfg->grid < 0) return GME_ERR_INVALID;
@@ -337,6 +376,100 @@ gme_status gme_align(gme_context *ctx, gme_kind kind, const int32_t *a, int64_t 
     ctx->ws.last_error = "device-side wait timed out";
     return to_status(out->status);
   }
+  return GME_OK;
+}
+
+// the plain path for the pairs a batch hands over (too wide for shared rows, or empty)
+static int batch_plain_cb(void *p, int kind, const int *d_a, long long n1, const int *d_b, long long n2,
+                          gme_result *d_out) {
+  struct Arg { gme_context *ctx; const gme_scoring *sc; cudaStream_t st; };
+  Arg *a = (Arg *)p;
+  return (int)gme_align_device(a->ctx, (gme_kind)kind, d_a, n1, d_b, n2, a->sc, d_out, nullptr,
+                               nullptr, a->st);
+}
+
+gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg) {
+  if (!ctx) return GME_ERR_INVALID;
+  gme::BatchTuning t;
+  if (cfg) {
+    if (cfg->warps_per_block) {
+      if (!gme::batch_config_valid(cfg->warps_per_block)) {
+        ctx->ws.last_error = "batch config: warps_per_block must be 4 or 8";
+        return GME_ERR_INVALID;
+      }
+      t.warps_per_block = cfg->warps_per_block;
+    }
+    if (cfg->blocks_per_sm < 0 || cfg->warp_max_rows < 0 || cfg->warp_max_cols < 0 ||
+        cfg->warp_max_cols > 1024)
+      return GME_ERR_INVALID;
+    t.blocks_per_sm = cfg->blocks_per_sm;
+    if (cfg->warp_max_rows) t.warp_max_rows = cfg->warp_max_rows;
+    if (cfg->warp_max_cols) t.warp_max_cols = cfg->warp_max_cols;
+  }
+  ctx->batch_tune = t;
+  return GME_OK;
+}
+
+gme_status gme_align_batch_device(gme_context *ctx, const int32_t *d_symbols, int64_t nsym,
+                                  const gme_pair *pairs, int64_t npairs, const gme_scoring *sc,
+                                  gme_result *d_results, void *stream) {
+  if (!ctx || npairs < 0 || (npairs > 0 && (!pairs || !d_results || !d_symbols)) || nsym < 0)
+    return GME_ERR_INVALID;
+  if (npairs == 0) return GME_OK;
+  gme_scoring def = gme_default_scoring();
+  if (!sc) sc = &def;
+  for (int64_t i = 0; i < npairs; ++i) {
+    gme_status s = check_sizes(ctx, (gme_kind)pairs[i].kind, pairs[i].n1, pairs[i].n2, sc);
+    if (s != GME_OK) {
+      ctx->ws.last_error = "pair " + std::to_string(i) + ": " + ctx->ws.last_error;
+      return s;
+    }
+  }
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  struct { gme_context *ctx; const gme_scoring *sc; cudaStream_t st; } arg = {ctx, sc, st};
+  int rc = gme::batch_run(ctx->ws, ctx->batch, d_symbols, nsym, pairs, npairs, to_scoring(sc),
+                          d_results, st, ctx->batch_tune, ctx->timeout_ns, batch_plain_cb, &arg);
+  return to_status(rc);
+}
+
+gme_status gme_align_batch(gme_context *ctx, const int32_t *symbols, int64_t nsym,
+                           const gme_pair *pairs, int64_t npairs, const gme_scoring *sc,
+                           gme_result *results) {
+  if (!ctx || npairs < 0 || nsym < 0 || (npairs > 0 && (!pairs || !results || !symbols)))
+    return GME_ERR_INVALID;
+  if (npairs == 0) return GME_OK;
+  cudaSetDevice(ctx->device);
+  int rc;
+  if ((rc = grow_dev((void **)&ctx->d_bsym, &ctx->d_bsym_cap, std::max<int64_t>(nsym, 1), 4, ctx)) ||
+      (rc = grow_dev((void **)&ctx->d_bres, &ctx->d_bres_cap, npairs, sizeof(gme_result), ctx)))
+    return to_status(rc);
+  cudaStream_t st = ctx->stream;
+  cudaError_t e;
+  if (nsym > 0 && (e = cudaMemcpyAsync(ctx->d_bsym, symbols, (size_t)nsym * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return to_status(ctx->ws.fail(e, "cudaMemcpyAsync(batch symbols)"));
+  gme_status s = gme_align_batch_device(ctx, ctx->d_bsym, nsym, pairs, npairs, sc, ctx->d_bres, st);
+  if (s != GME_OK) return s;
+  if ((e = cudaMemcpyAsync(results, ctx->d_bres, (size_t)npairs * sizeof(gme_result), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return to_status(ctx->ws.fail(e, "cudaMemcpyAsync(batch results)"));
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return to_status(ctx->ws.fail(e, "cudaStreamSynchronize"));
+  for (int64_t i = 0; i < npairs; ++i)
+    if (results[i].status != 0) {
+      ctx->ws.last_error = "device-side wait timed out";
+      return to_status(results[i].status);
+    }
+  int bad = 0;
+  if ((e = cudaMemcpy(&bad, ctx->batch.d_ctrl + 2, sizeof(int), cudaMemcpyDeviceToHost)) == cudaSuccess && bad)
+    return to_status(bad);
+  return GME_OK;
+}
+
+gme_status gme_batch_stats(const gme_context *ctx, int64_t *block_jobs, int64_t *warp_jobs,
+                           int64_t *long_jobs) {
+  if (!ctx) return GME_ERR_INVALID;
+  if (block_jobs) *block_jobs = ctx->batch.last_block_jobs;
+  if (warp_jobs) *warp_jobs = ctx->batch.last_warp_jobs;
+  if (long_jobs) *long_jobs = ctx->batch.last_long_jobs;
   return GME_OK;
 }
 

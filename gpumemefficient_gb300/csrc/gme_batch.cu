@@ -1,0 +1,558 @@
+// gme_batch.cu -- many alignments of uneven lengths and mixed kinds in one launch.
+//
+// One persistent work-queue kernel.  Its CTAs first take "block jobs" (a whole
+// pair per CTA: the CTA's NW warps are pipelined over the pair's row bands, band
+// b on warp b % NW, handing rows through shared rings; the last warp's row wraps
+// back to warp 0 for the next group of bands through a double-buffered row in
+// shared memory).  When the block queue is empty every warp takes "warp jobs"
+// on its own (a small pair swept band after band by one warp, its row kept in a
+// per-warp shared buffer).  Jobs are ordered longest first.  Pairs too wide for
+// the shared rows go to the plain path (one multi-CTA launch each, on the same
+// stream).  The cell engine is the plain kernel's (gme_engine.cuh), so results
+// are bit-exact with it and with the oracle.
+//
+// Replaces, for many pairs at once, the reference's one-pair-per-call host
+// functions (EditDistance/GPU_Hyperlane_Share.cu:689-789 and its LCS/SW twins).
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "gme_engine.cuh"
+#include "gme_internal.h"
+
+namespace gme {
+
+constexpr int BLOCK_MAXN = 4096;  // widest pair (n1) a block job keeps in shared memory
+constexpr int WARP_MAXN = 1024;   // widest pair a warp job keeps in shared memory
+// a row is read up to one chunk past the last chunk (the read-ahead): j_end+1 with
+// j_end = (n1 + 32R)/C, so a row of n1 columns needs n1 + 32R + 2C entries (R <= 8)
+constexpr int ROWSTRIDE_B = BLOCK_MAXN + 32 * 8 + 3 * C;
+constexpr int ROWSTRIDE_W = WARP_MAXN + 32 * 8 + 3 * C;
+
+struct BatchParams {
+  const int *sym;          // staged, padded symbols
+  const BatchJob *jobs_b;  // block jobs, longest first
+  const BatchJob *jobs_w;  // warp jobs, longest first
+  int n_b, n_w;
+  gme_result *results;
+  int *ctrl;  // [0] block ticket, [1] warp ticket, [2] status
+  Scoring sc;
+  unsigned long long timeout_ns;
+};
+
+template <int NW> struct __align__(16) BatchSmem {
+  int ring[NW][RING];       // ring[w]: warp w-1 -> warp w (w >= 1)
+  int tag[NW][RING / C];
+  int cons[NW];
+  union {
+    struct {
+      int row[2][ROWSTRIDE_B];  // warp NW-1 -> warp 0 across band groups
+      int tag[2][ROWSTRIDE_B / C];
+    } wrap;
+    int own[NW][ROWSTRIDE_W];  // warp jobs: each warp's own row
+  } u;
+  int job;
+  int abort;
+  SwBest best[NW];
+};
+
+// ---------------------------------------------------------------------------
+// Where a band's incoming row comes from and where its bottom row goes.  The mode
+// is uniform across the warp and fixed for a band, so the switches cost a
+// predictable branch per chunk and one sweep routine serves every combination.
+// ---------------------------------------------------------------------------
+enum : int { IN_TOP = 0, IN_RING = 1, IN_ROW = 2, IN_OWN = 3 };
+enum : int { OUT_NONE = 0, OUT_RING = 1, OUT_ROW = 2, OUT_OWN = 3 };
+
+struct Src {
+  int mode;
+  const int *buf;   // ring or row values
+  const int *tags;  // ring or row chunk tags
+  int *cons;        // ring: consumption counter (stream position)
+  int base;         // ring: stream position of column 0; row: tag generation
+  int rule;         // top border: ED boundary rule
+};
+
+struct Dst {
+  int mode;
+  int *buf;
+  int *tags;
+  const int *cons;
+  int base;
+  int cons_seen;
+};
+
+template <int KIND>
+__device__ __forceinline__ int src_tag(const Src &s, int j) {
+  if (s.mode == IN_RING) return ld_acquire_cta(&s.tags[(s.base / C + j) & (RING / C - 1)]);
+  if (s.mode == IN_ROW) return ld_acquire_cta(&s.tags[j]);
+  return 0;
+}
+__device__ __forceinline__ int src_want(const Src &s, int j) {
+  if (s.mode == IN_RING) return s.base / C + j + 1;
+  if (s.mode == IN_ROW) return s.base + j + 1;
+  return 0;
+}
+template <int KIND>
+__device__ __forceinline__ void src_load(const Src &s, int j, int (&d)[C]) {
+  if (s.mode == IN_TOP) {
+#pragma unroll
+    for (int k = 0; k < C; ++k) d[k] = Rec<KIND>::top(C * j + k, s.rule);
+    return;
+  }
+  const int *p = (s.mode == IN_RING) ? s.buf + ((s.base + C * j) & (RING - 1)) : s.buf + C * j;
+#pragma unroll
+  for (int k = 0; k < C; k += 4) {
+    const int4 q = *reinterpret_cast<const int4 *>(p + k);
+    d[k] = q.x; d[k + 1] = q.y; d[k + 2] = q.z; d[k + 3] = q.w;
+  }
+}
+
+__device__ __forceinline__ bool dst_put(Dst &o, int pos, const int (&q)[C], int lane, Waiter &W) {
+  if (o.mode == OUT_NONE) return true;
+  int *p;
+  if (o.mode == OUT_RING) {
+    const int sp = o.base + pos;
+    if (sp + C - RING > o.cons_seen) {
+      if (!W.wait([&] {
+            o.cons_seen = __shfl_sync(FULL, lds_vol(o.cons), 0);
+            return o.cons_seen >= sp + C - RING;
+          }))
+        return false;
+    }
+    p = o.buf + (sp & (RING - 1));
+  } else {
+    p = o.buf + pos;
+  }
+  if (lane == 31) {
+#pragma unroll
+    for (int k = 0; k < C; k += 4)
+      *reinterpret_cast<int4 *>(p + k) = make_int4(q[k], q[k + 1], q[k + 2], q[k + 3]);
+    if (o.mode == OUT_RING) st_release_cta(&o.tags[((o.base + pos) / C) & (RING / C - 1)], (o.base + pos) / C + 1);
+    else if (o.mode == OUT_ROW) st_release_cta(&o.tags[pos / C], o.base + pos / C + 1);
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// One warp sweeps one band (32*R rows starting at row y0+1) of one pair.
+// Returns false if a wait gave up.  On return `corner` (lane 31) holds the
+// stored value of the band's bottom row at column n1 and `tb` the lane's SW best.
+// ---------------------------------------------------------------------------
+template <int KIND, int R>
+__device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict__ a_sym,
+                                        const int *__restrict__ b_sym, int N, int M, int y0,
+                                        int lane, Src in, Dst out, Waiter &W, int &corner,
+                                        SwBest &tb) {
+  const Rec<KIND> rec(sc);
+  const int yl = y0 + lane * R + 1;  // first row of this lane
+  int bs[R], cur[R], prv[R], smax[R], sstep[R];
+#pragma unroll
+  for (int r = 0; r < R; r += 4) {
+    const int4 q = ldg4(b_sym + (yl - 1 + r));
+    bs[r] = q.x; bs[r + 1] = q.y; bs[r + 2] = q.z; bs[r + 3] = q.w;
+  }
+  unsigned padmask = 0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    cur[r] = Rec<KIND>::left(yl + r);
+    prv[r] = cur[r];
+    smax[r] = 0;
+    sstep[r] = 0;
+    if (yl + r > M) padmask |= 1u << r;
+  }
+  const bool padwarp = __any_sync(FULL, padmask != 0);
+
+  const int *sym = a_sym + (PADL - 1 - lane * R);
+  int win[2 * C];
+#pragma unroll
+  for (int k = 0; k < C; k += 4) {
+    const int4 q = ldg4(sym + k);
+    win[k] = q.x; win[k + 1] = q.y; win[k + 2] = q.z; win[k + 3] = q.w;
+  }
+#pragma unroll
+  for (int k = 0; k < R; k += 4) {
+    const int4 q = ldg4(sym - R + k);
+    win[2 * C - R + k] = q.x; win[2 * C - R + k + 1] = q.y;
+    win[2 * C - R + k + 2] = q.z; win[2 * C - R + k + 3] = q.w;
+  }
+#pragma unroll
+  for (int k = C; k < 2 * C - R; ++k) win[k] = 0;
+
+  int recv = 0, recv_prev = 0;
+  int ib[2][C];
+  int tag_next = src_tag<KIND>(in, 0);
+  src_load<KIND>(in, 0, ib[0]);
+
+  auto chunk = [&](int j, auto par, auto checked, auto padrows) -> bool {
+    constexpr int PAR = decltype(par)::value;
+    constexpr bool CK = decltype(checked)::value, PD = decltype(padrows)::value;
+    int(&inv)[C] = ib[PAR];
+    const int s0 = C * j;
+    __syncwarp();
+    if (s0 <= N && !__all_sync(FULL, tag_next == src_want(in, j))) {
+      auto ready = [&] { return __all_sync(FULL, src_tag<KIND>(in, j) == src_want(in, j)); };
+      if (!W.wait(ready)) return false;
+      src_load<KIND>(in, j, inv);
+    }
+    if (in.mode == IN_RING && lane == 31) sts_vol(in.cons, in.base + s0 + C);
+    if (lane == 0) recv = inv[0];
+    tag_next = src_tag<KIND>(in, j + 1);
+    src_load<KIND>(in, j + 1, ib[PAR ^ 1]);
+    int outq[C];
+    steps_chunk<KIND, R, PAR, CK, PD>(rec, cur, prv, recv, recv_prev, win, sym + s0 + C, bs, inv,
+                                      outq, s0, lane, N, padmask, smax, sstep);
+    const int pos = s0 - 32 * R;
+    if (pos >= 0 && !dst_put(out, pos, outq, lane, W)) return false;
+    return true;
+  };
+
+  using T = std::true_type;
+  using F = std::false_type;
+  using P0 = std::integral_constant<int, 0>;
+  using P1 = std::integral_constant<int, 1>;
+  auto range = [&](int ja, int jb, auto ck, auto pd) -> bool {
+    int j = ja;
+    if (j <= jb && (j & 1)) {
+      if (!chunk(j, P1{}, ck, pd)) return false;
+      ++j;
+    }
+    for (; j + 1 <= jb; j += 2) {
+      if (!chunk(j, P0{}, ck, pd)) return false;
+      if (!chunk(j + 1, P1{}, ck, pd)) return false;
+    }
+    if (j <= jb && !chunk(j, P0{}, ck, pd)) return false;
+    return true;
+  };
+  const int j_end = (N + 32 * R) / C;
+  if (padwarp) {
+    if (!range(0, j_end, T{}, T{})) return false;
+  } else {
+    const int j_lo = min((32 * R) / C, j_end + 1);
+    const int j_hi = max(min((N - C + 1) / C, j_end), j_lo - 1);
+    if (!range(0, j_lo - 1, T{}, F{})) return false;
+    if (!range(j_lo, j_hi, F{}, F{})) return false;
+    if (!range(j_hi + 1, j_end, T{}, F{})) return false;
+  }
+  corner = cur[R - 1];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const long long y = yl + r;
+    if (KIND == K_SW && y <= M && smax[r] > 0) {
+      SwBest c = {smax[r], 0, y, (long long)(sstep[r] - lane * R - r)};
+      if (better(c, tb)) tb = c;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ SwBest warp_best(SwBest b) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    SwBest c;
+    c.v = __shfl_down_sync(FULL, b.v, o);
+    c.y = __shfl_down_sync(FULL, b.y, o);
+    c.x = __shfl_down_sync(FULL, b.x, o);
+    c.pad = 0;
+    if (better(c, b)) b = c;
+  }
+  return b;
+}
+
+// A whole pair on one CTA: warp w sweeps bands w, w+NW, w+2NW, ...; band b takes
+// its incoming row from warp b-1 (ring[w]) or, for w = 0, from the wrap row the
+// last warp wrote in the previous group.
+template <int KIND, int R, int NW>
+__device__ void block_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob &jb, int warp,
+                          int lane, Waiter &W) {
+  const int N = jb.n1, M = jb.n2;
+  const int *a_sym = P.sym + jb.a_off;
+  const int *b_sym = P.sym + jb.b_off;
+  const int nb = (M + 32 * R - 1) / (32 * R);
+  const int L = ((N + 1 + C - 1) / C) * C + 2 * C;  // stream positions per band row
+  SwBest tb = {0, 0, 0, 0};
+  int corner = 0, corner_band = -1;
+  bool ok = true;
+  for (int g = 0; ok && g * NW + warp < nb; ++g) {
+    const int band = g * NW + warp;
+    Src in;
+    in.rule = P.sc.ed_rule;
+    if (band == 0) {
+      in.mode = IN_TOP;
+    } else if (warp == 0) {
+      in.mode = IN_ROW; in.buf = S.u.wrap.row[(g - 1) & 1]; in.tags = S.u.wrap.tag[(g - 1) & 1];
+      in.base = (g - 1) * (L / C);
+    } else {
+      in.mode = IN_RING; in.buf = S.ring[warp]; in.tags = S.tag[warp]; in.cons = &S.cons[warp];
+      in.base = g * L;
+    }
+    Dst out;
+    out.cons_seen = 0;
+    if (band == nb - 1) {
+      out.mode = OUT_NONE;
+    } else if (warp == NW - 1) {
+      out.mode = OUT_ROW; out.buf = S.u.wrap.row[g & 1]; out.tags = S.u.wrap.tag[g & 1];
+      out.base = g * (L / C);
+    } else {
+      out.mode = OUT_RING; out.buf = S.ring[warp + 1]; out.tags = S.tag[warp + 1];
+      out.cons = &S.cons[warp + 1]; out.base = g * L;
+    }
+    int c = 0;
+    ok = sweep_band<KIND, R>(P.sc, a_sym, b_sym, N, M, band * 32 * R, lane, in, out, W, c, tb);
+    if (band == nb - 1) { corner = c; corner_band = band; }
+  }
+  // results: the corner from the warp that swept the last band, SW best over the CTA
+  if (KIND == K_SW) {
+    tb = warp_best(tb);
+    if (lane == 0) S.best[warp] = tb;
+  }
+  __syncthreads();
+  if (corner_band >= 0 && lane == 31) {
+    gme_result r;
+    r.score = Rec<KIND>::to_v(corner, N, M);
+    SwBest b = {0, 0, 0, 0};
+    if (KIND == K_SW)
+      for (int k = 0; k < NW; ++k)
+        if (better(S.best[k], b)) b = S.best[k];
+    r.sw_max = b.v;
+    r.sw_max_y = b.y;
+    r.sw_max_x = b.x;
+    r.status = 0;
+    r.kind = KIND;
+    P.results[jb.index] = r;
+  }
+}
+
+// A small pair on one warp: bands one after another through the warp's own row.
+template <int KIND, int R, int NW>
+__device__ void warp_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob &jb, int warp,
+                         int lane, Waiter &W) {
+  const int N = jb.n1, M = jb.n2;
+  const int *a_sym = P.sym + jb.a_off;
+  const int *b_sym = P.sym + jb.b_off;
+  const int nb = (M + 32 * R - 1) / (32 * R);
+  int *row = S.u.own[warp];
+  SwBest tb = {0, 0, 0, 0};
+  int corner = 0;
+  for (int band = 0; band < nb; ++band) {
+    Src in;
+    in.rule = P.sc.ed_rule;
+    in.mode = band == 0 ? IN_TOP : IN_OWN;
+    in.buf = row;
+    Dst out;
+    out.cons_seen = 0;
+    out.mode = band == nb - 1 ? OUT_NONE : OUT_OWN;
+    out.buf = row;
+    if (!sweep_band<KIND, R>(P.sc, a_sym, b_sym, N, M, band * 32 * R, lane, in, out, W, corner, tb))
+      return;
+  }
+  if (KIND == K_SW) tb = warp_best(tb);
+  SwBest b0;
+  b0.v = __shfl_sync(FULL, tb.v, 0);
+  b0.y = __shfl_sync(FULL, tb.y, 0);
+  b0.x = __shfl_sync(FULL, tb.x, 0);
+  if (lane == 31) {
+    gme_result r;
+    r.score = Rec<KIND>::to_v(corner, N, M);
+    r.sw_max = KIND == K_SW ? b0.v : 0;
+    r.sw_max_y = KIND == K_SW ? b0.y : 0;
+    r.sw_max_x = KIND == K_SW ? b0.x : 0;
+    r.status = 0;
+    r.kind = KIND;
+    P.results[jb.index] = r;
+  }
+}
+
+template <int R, int NW>
+__global__ void __launch_bounds__(NW * 32) batch_kernel(BatchParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  BatchSmem<NW> &S = *reinterpret_cast<BatchSmem<NW> *>(smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) S.abort = 0;
+  __syncthreads();
+  Waiter W(P.timeout_ns, &P.ctrl[2], &S.abort);
+  // phase 1: block jobs, one pair per CTA
+  for (;;) {
+    if (threadIdx.x == 0) S.job = S.abort ? P.n_b : atomicAdd(&P.ctrl[0], 1);
+    for (int i = threadIdx.x; i < NW * (RING / C); i += blockDim.x) (&S.tag[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < NW; i += blockDim.x) S.cons[i] = 0;
+    for (int i = threadIdx.x; i < 2 * (ROWSTRIDE_B / C); i += blockDim.x) (&S.u.wrap.tag[0][0])[i] = 0;
+    __syncthreads();
+    const int t = S.job;
+    if (t >= P.n_b) break;
+    const BatchJob jb = P.jobs_b[t];
+    switch (jb.kind) {
+      case K_LCS: block_job<K_LCS, R, NW>(P, S, jb, warp, lane, W); break;
+      case K_ED: block_job<K_ED, R, NW>(P, S, jb, warp, lane, W); break;
+      default: block_job<K_SW, R, NW>(P, S, jb, warp, lane, W); break;
+    }
+    __syncthreads();
+  }
+  // phase 2: warp jobs, one small pair per warp
+  for (;;) {
+    int t = 0;
+    if (lane == 0) t = S.abort ? P.n_w : atomicAdd(&P.ctrl[1], 1);
+    t = __shfl_sync(FULL, t, 0);
+    if (t >= P.n_w) break;
+    const BatchJob jb = P.jobs_w[t];
+    switch (jb.kind) {
+      case K_LCS: warp_job<K_LCS, R, NW>(P, S, jb, warp, lane, W); break;
+      case K_ED: warp_job<K_ED, R, NW>(P, S, jb, warp, lane, W); break;
+      default: warp_job<K_SW, R, NW>(P, S, jb, warp, lane, W); break;
+    }
+    if (*(volatile int *)&S.abort) break;
+  }
+}
+
+// Copies every pair's sequences into the padded, aligned layout the engine reads.
+__global__ void batch_stage_kernel(const int *__restrict__ src, const long long *__restrict__ from,
+                                   const long long *__restrict__ to, const int *__restrict__ len,
+                                   const int *__restrict__ padl, const int *__restrict__ total,
+                                   int nseg, int *__restrict__ dst) {
+  for (int s = blockIdx.x; s < nseg; s += gridDim.x) {
+    const long long f = from[s], t0 = to[s];
+    const int n = len[s], pl = padl[s], tot = total[s];
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+      const int k = i - pl;
+      dst[t0 + i] = (k >= 0 && k < n) ? src[f + k] : 0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side: plan (classify, order, lay out), stage, launch.
+// ---------------------------------------------------------------------------
+template <int R, int NW>
+static cudaError_t launch_batch_t(const BatchParams &P, int grid, cudaStream_t st) {
+  const size_t smem = sizeof(BatchSmem<NW>);
+  cudaError_t e = cudaFuncSetAttribute(batch_kernel<R, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  batch_kernel<R, NW><<<grid, NW * 32, smem, st>>>(P);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_batch(int NW, const BatchParams &P, int grid, cudaStream_t st) {
+  switch (NW) {
+    case 4: return launch_batch_t<4, 4>(P, grid, st);
+    case 8: return launch_batch_t<4, 8>(P, grid, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <int R, int NW>
+static int occupancy_t() {
+  int n = 0;
+  const size_t smem = sizeof(BatchSmem<NW>);
+  cudaFuncSetAttribute(batch_kernel<R, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<R, NW>, NW * 32, smem);
+  return n;
+}
+
+int batch_occupancy(int NW) {
+  switch (NW) {
+    case 4: return occupancy_t<4, 4>();
+    case 8: return occupancy_t<4, 8>();
+  }
+  return 0;
+}
+
+bool batch_config_valid(int NW) { return NW == 4 || NW == 8; }
+
+int batch_run(Workspace &ws, BatchArena &ar, const int *d_sym, long long nsym, const gme_pair *pairs,
+              long long npairs, const Scoring &sc, gme_result *d_results, cudaStream_t st,
+              const BatchTuning &tune, unsigned long long timeout_ns,
+              int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *),
+              void *plain_ctx) {
+  constexpr int R = 4;
+  const int NW = tune.warps_per_block;
+  if (!batch_config_valid(NW)) return ws.fail_msg(ST_INVALID, "batch: warps_per_block must be 4 or 8");
+  // classify
+  std::vector<int> blockj, warpj, longj;
+  for (long long i = 0; i < npairs; ++i) {
+    const gme_pair &p = pairs[i];
+    if (p.n1 < 0 || p.n2 < 0 || p.kind < 0 || p.kind > 2 || p.a_off < 0 || p.b_off < 0 ||
+        p.a_off + p.n1 > nsym || p.b_off + p.n2 > nsym)
+      return ws.fail_msg(ST_INVALID, "batch: pair " + std::to_string(i) + " out of range");
+    if (p.n1 == 0 || p.n2 == 0 || p.n1 > BLOCK_MAXN) longj.push_back((int)i);
+    else if (p.n1 <= WARP_MAXN && p.n1 <= tune.warp_max_cols && p.n2 <= tune.warp_max_rows) warpj.push_back((int)i);
+    else blockj.push_back((int)i);
+  }
+  auto by_cells = [&](int x, int y) {
+    const long long cx = (long long)pairs[x].n1 * pairs[x].n2, cy = (long long)pairs[y].n1 * pairs[y].n2;
+    return cx != cy ? cx > cy : x < y;
+  };
+  std::sort(blockj.begin(), blockj.end(), by_cells);
+  std::sort(warpj.begin(), warpj.end(), by_cells);
+  // staged layout: a padded with PADL/PADR at a 16-byte aligned start, b padded to whole bands
+  const long long nseg = 2 * (long long)(blockj.size() + warpj.size());
+  ar.h_from.resize(nseg); ar.h_to.resize(nseg); ar.h_len.resize(nseg); ar.h_padl.resize(nseg); ar.h_total.resize(nseg);
+  ar.h_jobs.resize(blockj.size() + warpj.size());
+  long long off = 0, seg = 0;
+  auto place = [&](long long from, int len, int padl, int total) {
+    ar.h_from[seg] = from; ar.h_to[seg] = off; ar.h_len[seg] = len; ar.h_padl[seg] = padl; ar.h_total[seg] = total;
+    ++seg;
+    const long long at = off;
+    off += (total + 3) / 4 * 4;
+    return at;
+  };
+  auto add = [&](int i, int rows_mult, size_t slot) {
+    const gme_pair &p = pairs[i];
+    BatchJob j;
+    j.a_off = place(p.a_off, p.n1, PADL, PADL + p.n1 + PADR);
+    const int brows = (p.n2 + rows_mult - 1) / rows_mult * rows_mult;
+    j.b_off = place(p.b_off, p.n2, 0, brows);
+    j.n1 = p.n1; j.n2 = p.n2; j.kind = p.kind; j.index = i;
+    ar.h_jobs[slot] = j;
+  };
+  size_t slot = 0;
+  for (int i : blockj) add(i, 32 * R * NW, slot++);
+  for (int i : warpj) add(i, 32 * R, slot++);
+  const long long staged = off + 64;
+  int rc = ar.reserve(staged, nseg, (long long)ar.h_jobs.size(), ws);
+  if (rc != ST_OK) return rc;
+  cudaError_t e;
+  if (nseg > 0) {
+    if ((e = cudaMemcpyAsync(ar.d_from, ar.h_from.data(), nseg * 8, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(ar.d_to, ar.h_to.data(), nseg * 8, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(ar.d_len, ar.h_len.data(), nseg * 4, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(ar.d_padl, ar.h_padl.data(), nseg * 4, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(ar.d_total, ar.h_total.data(), nseg * 4, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(ar.d_jobs, ar.h_jobs.data(), ar.h_jobs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice, st)))
+      return ws.fail(e, "cudaMemcpyAsync(batch plan)");
+    // the host vectors must outlive the copies
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return ws.fail(e, "cudaStreamSynchronize(batch plan)");
+    const int blocks = (int)std::min<long long>(nseg, 65535);
+    batch_stage_kernel<<<blocks, 256, 0, st>>>(d_sym, ar.d_from, ar.d_to, ar.d_len, ar.d_padl, ar.d_total, (int)nseg, ar.d_staged);
+    ws.launches += 1;
+    if ((e = cudaGetLastError()) != cudaSuccess) return ws.fail(e, "batch_stage_kernel");
+    if ((e = cudaMemsetAsync(ar.d_ctrl, 0, 4 * sizeof(int), st)) != cudaSuccess) return ws.fail(e, "cudaMemsetAsync(batch ctrl)");
+    BatchParams P;
+    P.sym = ar.d_staged;
+    P.jobs_b = reinterpret_cast<const BatchJob *>(ar.d_jobs);
+    P.jobs_w = P.jobs_b + blockj.size();
+    P.n_b = (int)blockj.size();
+    P.n_w = (int)warpj.size();
+    P.results = d_results;
+    P.ctrl = ar.d_ctrl;
+    P.sc = sc;
+    P.timeout_ns = timeout_ns;
+    int occ = batch_occupancy(NW);
+    if (occ < 1) occ = 1;
+    int grid = ws.sms * std::min(occ, tune.blocks_per_sm > 0 ? tune.blocks_per_sm : occ);
+    if ((e = launch_batch(NW, P, grid, st)) != cudaSuccess) return ws.fail(e, "batch_kernel");
+    ws.launches += 1;
+  }
+  // pairs the shared-memory rows cannot hold: the plain path, one launch each
+  for (int i : longj) {
+    const gme_pair &p = pairs[i];
+    rc = plain(plain_ctx, p.kind, d_sym + p.a_off, p.n1, d_sym + p.b_off, p.n2, d_results + i);
+    if (rc != ST_OK) return rc;
+  }
+  ar.last_block_jobs = (long long)blockj.size();
+  ar.last_warp_jobs = (long long)warpj.size();
+  ar.last_long_jobs = (long long)longj.size();
+  return ST_OK;
+}
+
+}  // namespace gme

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <vector>
 
 #include "gme.h"
 
@@ -36,6 +37,46 @@ struct Workspace {
   int fail_msg(int status, const std::string &msg);
   void release();
 };
+
+// One job of a batch as the batched kernel reads it.
+struct BatchJob {
+  long long a_off;  // staged a: symbols at a_off + PADL + i
+  long long b_off;  // staged b: symbols at b_off + i, padded to whole bands
+  int n1, n2;
+  int kind;
+  int index;  // result slot
+};
+
+struct BatchTuning {
+  int warps_per_block = 4;  // compute warps of a CTA (block jobs pipeline them over bands)
+  int blocks_per_sm = 0;    // 0 = as many as fit
+  int warp_max_rows = 512;  // pairs up to this many rows (and up to 1024 columns) run one per warp
+  int warp_max_cols = 1024;
+};
+
+// Device and host buffers of the batched path, owned by a context, grown on demand.
+struct BatchArena {
+  std::vector<long long> h_from, h_to;
+  std::vector<int> h_len, h_padl, h_total;
+  std::vector<BatchJob> h_jobs;
+  int *d_staged = nullptr; long long staged_cap = 0;
+  long long *d_from = nullptr, *d_to = nullptr;
+  int *d_len = nullptr, *d_padl = nullptr, *d_total = nullptr; long long seg_cap = 0;
+  BatchJob *d_jobs = nullptr; long long jobs_cap = 0;
+  int *d_ctrl = nullptr;
+  long long last_block_jobs = 0, last_warp_jobs = 0, last_long_jobs = 0;
+  int reserve(long long staged, long long nseg, long long njobs, Workspace &ws);
+  void release();
+};
+
+// batched path (gme_batch.cu)
+bool batch_config_valid(int NW);
+int batch_occupancy(int NW);
+int batch_run(Workspace &ws, BatchArena &ar, const int *d_sym, long long nsym, const gme_pair *pairs,
+              long long npairs, const Scoring &sc, gme_result *d_results, cudaStream_t st,
+              const BatchTuning &tune, unsigned long long timeout_ns,
+              int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *),
+              void *plain_ctx);
 
 // plain path (gme_plain.cu)
 bool plain_config_valid(int R, int NW);

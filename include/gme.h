@@ -74,7 +74,7 @@ typedef struct gme_result {
 
 /* Tuning of the plain (one pair per call) wavefront kernel. Zero fields = automatic. */
 typedef struct gme_plain_config {
-  int32_t rows_per_lane;   /* cells of one anti-diagonal held per thread: 4 or 8 */
+  int32_t rows_per_lane;   /* cells of one anti-diagonal held per thread: 4 */
   int32_t warps_per_band;  /* compute warps per CTA; band height = warps*32*rows_per_lane */
   int32_t grid;            /* persistent CTAs (0 = one per band, capped by residency) */
   int32_t reserved;
@@ -113,6 +113,43 @@ gme_status gme_align_device(gme_context *ctx, gme_kind kind, const int32_t *d_a,
                             const int32_t *d_b, int64_t n2, const gme_scoring *sc,
                             gme_result *d_out, int32_t *d_last_row, int32_t *d_last_col,
                             void *stream);
+
+/* ---- batched path: many alignments in one launch --------------------------------
+ * Pair i reads a = symbols[a_off .. a_off+n1), b = symbols[b_off .. b_off+n2) and
+ * computes `kind` with the shared scoring; result i gets its score (and SW maximum).
+ * One persistent work-queue kernel runs every pair whose n1 <= 4096: pairs with
+ * n2 <= warp_max_rows and n1 <= warp_max_cols one per warp, the rest one per CTA
+ * (the CTA's warps pipelined over the pair's bands), longest first.  Wider or empty
+ * pairs run on the plain path, one launch each, on the same stream.  Replaces calling
+ * the reference's one-pair host function (e.g. EditDistance/GPU_Hyperlane_Share.cu:689)
+ * once per pair. */
+typedef struct gme_pair {
+  int64_t a_off, b_off; /* element offsets into the symbol buffer */
+  int32_t n1, n2;       /* lengths of a (columns) and b (rows) */
+  int32_t kind;         /* gme_kind */
+  int32_t reserved;
+} gme_pair;
+
+typedef struct gme_batch_config {
+  int32_t warps_per_block; /* 4 or 8 (0 = automatic) */
+  int32_t blocks_per_sm;   /* CTAs per SM (0 = as many as fit) */
+  int32_t warp_max_rows;   /* pairs with n2 <= this (and n1 <= warp_max_cols) run one per warp */
+  int32_t warp_max_cols;   /* at most 1024 */
+} gme_batch_config;
+
+gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg);
+/* Host buffers; blocks until all results are in `results`. */
+gme_status gme_align_batch(gme_context *ctx, const int32_t *symbols, int64_t nsym,
+                           const gme_pair *pairs, int64_t npairs, const gme_scoring *sc,
+                           gme_result *results);
+/* Device symbols and results, host pair list (the plan is made on the host).
+ * Returns once the work is queued on `stream`. */
+gme_status gme_align_batch_device(gme_context *ctx, const int32_t *d_symbols, int64_t nsym,
+                                  const gme_pair *pairs, int64_t npairs, const gme_scoring *sc,
+                                  gme_result *d_results, void *stream);
+/* How the last batch was split: one-per-CTA, one-per-warp and plain-path pairs. */
+gme_status gme_batch_stats(const gme_context *ctx, int64_t *block_jobs, int64_t *warp_jobs,
+                           int64_t *long_jobs);
 
 /* ---- plain path without allocation --------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc (code

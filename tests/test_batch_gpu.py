@@ -1,0 +1,89 @@
+"""Parity of the batched path (one launch, many uneven mixed pairs) with the oracle."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def check_batch(ctx, kinds, sa, sb, rule=0, sc=None):
+    import gpumemefficient_gb300 as g
+    sc = sc or g.scoring(ed_boundary=rule)
+    res = ctx.align_batch(kinds, sa, sb, sc=sc)
+    o = O.align_batch(kinds, sa, sb, rule=rule, match=sc.match, mismatch=sc.mismatch, gap=sc.gap)
+    np.testing.assert_array_equal(res["status"], 0)
+    np.testing.assert_array_equal(res["score"], o["score"])
+    sw = np.asarray(kinds) == 2
+    np.testing.assert_array_equal(res["sw_max"][sw], o["sw_max"][sw])
+    np.testing.assert_array_equal(res["sw_max_y"][sw], o["sw_y"][sw])
+    np.testing.assert_array_equal(res["sw_max_x"][sw], o["sw_x"][sw])
+    return res
+
+
+@pytest.mark.parametrize("nw", [4, 8])
+def test_mixed_uneven(gme_ctx, nw):
+    rng = np.random.default_rng(31 + nw)
+    n = 600
+    kinds = rng.integers(0, 3, n)
+    la = np.exp(rng.uniform(np.log(1), np.log(3000), n)).astype(int)
+    lb = np.exp(rng.uniform(np.log(1), np.log(3000), n)).astype(int)
+    sa = [rng.integers(0, 4, k) for k in la]
+    sb = [rng.integers(0, 4, k) for k in lb]
+    gme_ctx.set_batch_config(warps_per_block=nw)
+    try:
+        check_batch(gme_ctx, kinds, sa, sb, rule=0)
+        check_batch(gme_ctx, kinds, sa, sb, rule=1)
+        st = gme_ctx.batch_stats()
+        assert st["block_jobs"] > 0 and st["warp_jobs"] > 0
+    finally:
+        gme_ctx.set_batch_config()
+
+
+def test_shapes_edges(gme_ctx):
+    rng = np.random.default_rng(77)
+    shapes = [(1, 1), (1, 5), (5, 1), (0, 4), (4, 0), (0, 0), (1024, 512), (1025, 513), (4096, 4096),
+              (4097, 100), (100, 4097), (513, 2000), (2000, 513), (128, 128), (129, 127), (7000, 300)]
+    kinds, sa, sb = [], [], []
+    for i, (n1, n2) in enumerate(shapes):
+        for k in range(3):
+            kinds.append(k)
+            sa.append(rng.integers(0, 20, n1))
+            sb.append(rng.integers(0, 20, n2))
+    check_batch(gme_ctx, kinds, sa, sb)
+    st = gme_ctx.batch_stats()
+    assert st["long_jobs"] > 0
+
+
+def test_identical_and_disjoint(gme_ctx):
+    rng = np.random.default_rng(5)
+    kinds, sa, sb = [], [], []
+    for n in (100, 700, 2500):
+        a = rng.integers(0, 4, n)
+        for k in range(3):
+            kinds += [k, k]
+            sa += [a, np.zeros(n, int)]
+            sb += [a.copy(), np.ones(n + 3, int)]
+    check_batch(gme_ctx, kinds, sa, sb)
+
+
+def test_batch_sw_scoring(gme_ctx):
+    import gpumemefficient_gb300 as g
+    rng = np.random.default_rng(9)
+    kinds = [2] * 40
+    sa = [rng.integers(0, 6, rng.integers(50, 1500)) for _ in kinds]
+    sb = [rng.integers(0, 6, rng.integers(50, 1500)) for _ in kinds]
+    check_batch(gme_ctx, kinds, sa, sb, sc=g.scoring(5, -4, -7))
+
+
+def test_warp_cutoffs(gme_ctx):
+    rng = np.random.default_rng(12)
+    kinds = rng.integers(0, 3, 200)
+    sa = [rng.integers(0, 4, rng.integers(10, 1100)) for _ in kinds]
+    sb = [rng.integers(0, 4, rng.integers(10, 1100)) for _ in kinds]
+    for rows, cols in [(128, 256), (1024, 1024), (4096, 1024)]:
+        gme_ctx.set_batch_config(warp_max_rows=rows, warp_max_cols=cols)
+        try:
+            check_batch(gme_ctx, kinds, sa, sb)
+        finally:
+            gme_ctx.set_batch_config()
