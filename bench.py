@@ -10,7 +10,10 @@ resident in HBM; `e2e` is the same metric through the C ABI with host buffers
 (host->device copies and the device->host result read inside the timed region).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gme|reference]
-                  [--workload ed65536|lcs8192|sw32768|lcs32768]
+                  [--workload ed65536|lcs8192|sw32768|lcs32768|batched]
+
+The batched workload is 16384 pairs, each length log-uniform in [64, 4096], kinds
+LCS/ED/SW one third each, all in one planned launch replayed as a CUDA graph.
 """
 from __future__ import annotations
 
@@ -136,6 +139,8 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
+    if args.workload == "batched":
+        return run_reference_batch(args, ws)
     kind, a, b, cfg = workload(args.workload)
     from oracle import oracle as O
     threads = os.cpu_count() or 1
@@ -157,6 +162,36 @@ def run_reference(args):
             "cpu_baseline": {"value": val, "unit": "GCUPS", "cores": threads, "kind": "port",
                              "sample": f"{KIND_NAME[kind]} {len(a)} columns x {rows} rows per step "
                                        f"({cells:.3g} cells), oracle/oracle.c on {threads} threads"},
+            "e2e": {"value": val, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_batch(args, ws):
+    """Reference arm, batched workload: the CPU recurrence over a bounded sample of the pairs."""
+    from gpumemefficient_gb300 import synth
+    from oracle import oracle as O
+    kinds, sa, sb = synth.batch_pairs(args.pairs)
+    threads = os.cpu_count() or 1
+    k = min(len(kinds), 1500)
+    cells = float(sum(len(a) * len(b) for a, b in zip(sa[:k], sb[:k])))
+    for _ in range(args.warmup):
+        O.align_batch(kinds[:k], sa[:k], sb[:k], threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.align_batch(kinds[:k], sa[:k], sb[:k], threads=threads)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    val = cells * len(times) / tot / 1e9
+    cfg = {"workload": f"batched: {len(kinds)} pairs, lengths log-uniform [64, 4096], alphabet 4, "
+                       "LCS/ED/SW 1/3 each", "pairs": len(kinds), "seed": synth.SEED_BATCH}
+    line = {"impl": "reference", "metric": "GCUPS on 1 GB300 (bit-exact)", "value": val, "unit": "GCUPS",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded)", "config": cfg,
+            "cpu_baseline": {"value": val, "unit": "GCUPS", "cores": threads, "kind": "port",
+                             "sample": f"first {k} pairs per step ({cells:.3g} cells), oracle/oracle.c "
+                                       f"pairs across {threads} threads"},
             "e2e": {"value": val, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -277,6 +312,156 @@ def run_gme(args):
         torch.distributed.destroy_process_group()
 
 
+def run_gme_batch(args):
+    """16384 uneven mixed pairs in one planned launch (CUDA-graph replay)."""
+    import ctypes
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    import __graft_entry__ as ge
+    ge.build()
+    import gpumemefficient_gb300 as g
+    from gpumemefficient_gb300 import synth
+    from oracle import oracle as O
+
+    kinds, sa, sb = synth.batch_pairs(args.pairs)
+    symbols, pairs = g.pack_batch(kinds, sa, sb)
+    n = len(pairs)
+    cells_k = np.array([len(a) * len(b) for a, b in zip(sa, sb)], np.float64)
+    cells = float(cells_k.sum())
+    ops = float(sum(cells_k[np.asarray(kinds) == k].sum() * OPS_PER_CELL[k] for k in range(3)))
+    ctx = g.Context(local)
+    if args.batch_warps:
+        ctx.set_batch_config(warps_per_block=args.batch_warps)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=local)
+    sp = stream.cuda_stream
+    with torch.cuda.stream(stream):
+        d_sym = torch.from_numpy(symbols).to(dev)
+        d_res = torch.zeros(n * g.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+        flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream.synchronize()
+    plan = g.BatchPlan(ctx, pairs, len(symbols))
+    split = ctx.batch_stats()
+
+    # parity of every pair with the oracle (outside the timed region)
+    plan.run(d_sym.data_ptr(), d_res.data_ptr(), stream=sp)
+    stream.synchronize()
+    res = np.frombuffer(d_res.cpu().numpy().tobytes(), g.RESULT_DTYPE)
+    o = O.align_batch(kinds, sa, sb, threads=os.cpu_count() or 1)
+    sw = np.asarray(kinds) == 2
+    parity = bool((res["status"] == 0).all() and (res["score"] == o["score"]).all() and
+                  (res["sw_max"][sw] == o["sw_max"][sw]).all() and (res["sw_max_y"][sw] == o["sw_y"][sw]).all()
+                  and (res["sw_max_x"][sw] == o["sw_x"][sw]).all())
+
+    for _ in range(args.warmup):
+        plan.run(d_sym.data_ptr(), d_res.data_ptr(), stream=sp, use_graph=True)
+    stream.synchronize()
+    clocks = ClockSampler(local)
+    time.sleep(0.15)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches0 = ctx.launches
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            plan.run(d_sym.data_ptr(), d_res.data_ptr(), stream=sp, use_graph=True)
+            ends[i].record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launches - launches0
+    clk = clocks.stop()
+    step_ms = [s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)]
+    t_dev = sum(step_ms) / 1e3
+    if ws > 1:
+        t = torch.tensor([t_dev], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(t.item())
+    value = ws * cells * args.steps / t_dev / 1e9
+    mean_s = t_dev / args.steps
+
+    # end to end through the C ABI: pinned host symbols in, results out, plan made per call
+    hsym = torch.from_numpy(symbols).pin_memory().numpy()
+    hres = np.zeros(n, g.RESULT_DTYPE)
+    sc = g.scoring()
+    L = g.lib()
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(2):
+        L.gme_align_batch(ctx.handle, hsym.ctypes.data, len(hsym), pairs.ctypes.data, n, ctypes.byref(sc),
+                          hres.ctypes.data)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        st_ = L.gme_align_batch(ctx.handle, hsym.ctypes.data, len(hsym), pairs.ctypes.data, n,
+                                ctypes.byref(sc), hres.ctypes.data)
+    t_e2e = time.perf_counter() - t0
+    e2e = {"value": ws * cells * e2e_steps / t_e2e / 1e9, "unit": "GCUPS",
+           "h2d_bytes_per_step": int(hsym.nbytes + pairs.nbytes), "d2h_bytes_per_step": int(hres.nbytes),
+           "steps": e2e_steps, "scores_ok": bool(st_ == 0 and (hres["score"] == o["score"]).all())}
+
+    # the plain per-pair path on a spread subset of the same pairs
+    sub = np.arange(0, n, max(1, n // args.plain_sample))
+    d_one = torch.zeros(32, dtype=torch.uint8, device=dev)
+    offs = pairs[sub]
+    for _ in range(2):
+        for i in sub[:8]:
+            ctx.align_device(int(kinds[i]), d_sym.data_ptr() + 4 * int(pairs[i]["a_off"]), int(pairs[i]["n1"]),
+                             d_sym.data_ptr() + 4 * int(pairs[i]["b_off"]), int(pairs[i]["n2"]), d_one.data_ptr(), stream=sp)
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in sub:
+        ctx.align_device(int(kinds[i]), d_sym.data_ptr() + 4 * int(pairs[i]["a_off"]), int(pairs[i]["n1"]),
+                         d_sym.data_ptr() + 4 * int(pairs[i]["b_off"]), int(pairs[i]["n2"]), d_one.data_ptr(), stream=sp)
+    e1.record(stream)
+    stream.synchronize()
+    plain_gcups = float(cells_k[sub].sum()) / (e0.elapsed_time(e1) / 1e3) / 1e9
+    del offs
+
+    props = torch.cuda.get_device_properties(local)
+    sms = props.multi_processor_count
+    mhz = clk.get("sm_mhz") or 1920.0
+    peak_tops = sms * INT_LANES_PER_SM * mhz * 1e6 / 1e12
+    achieved = ops / mean_s / 1e12
+    roof = {"bound": "int_alu", "achieved": achieved, "peak": peak_tops, "unit": "Tops/s",
+            "frac": achieved / peak_tops, "traffic": None,
+            "peak_basis": f"{sms} SMs x {INT_LANES_PER_SM} INT32 lanes x median SM clock {mhz:.0f} MHz under load",
+            "ops_per_cell": "LCS 4, ED 7, SW 8 weighted by cells", "kernel": "batch_kernel (whole graph timed)"}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        k = min(n, 3000)
+        t0 = time.perf_counter()
+        O.align_batch(kinds[:k], sa[:k], sb[:k], threads=os.cpu_count() or 1)
+        dt = time.perf_counter() - t0
+        cpu = {"value": float(cells_k[:k].sum()) / dt / 1e9, "unit": "GCUPS", "cores": os.cpu_count(),
+               "kind": "port", "sample": f"first {k} of the {n} pairs ({cells_k[:k].sum():.3g} cells), "
+                                         f"oracle/oracle.c pairs across {os.cpu_count()} threads, {dt:.2f} s"}
+    cfg = {"workload": f"batched: {n} pairs, lengths log-uniform [64, 4096], alphabet 4, LCS/ED/SW 1/3 each, "
+                       "one planned launch replayed as a CUDA graph",
+           "pairs": n, "cells": cells, "seed": synth.SEED_BATCH, "split": split,
+           "l2": "flushed between timed steps (256 MiB write)", "parity_vs_oracle": "ok" if parity else "MISMATCH",
+           "plain_per_pair_gcups": plain_gcups, "plain_sample_pairs": int(len(sub)),
+           "batched_over_plain": value / ws / plain_gcups}
+    line = {"metric": "GCUPS on 1 GB300 (bit-exact)", "value": value, "unit": "GCUPS", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * mean_s,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded)", "config": cfg, "clocks": clk, "e2e": e2e,
+            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
+            "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    plan.close()
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -285,11 +470,17 @@ def main():
     p.add_argument("--impl", default="gme", choices=["gme", "reference"])
     p.add_argument("--workload", default="ed65536")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--pairs", type=int, default=16384, help="batched workload: number of pairs")
+    p.add_argument("--plain-sample", type=int, default=256,
+                   help="batched workload: pairs timed one by one on the plain path")
+    p.add_argument("--batch-warps", type=int, default=0, help="batched workload: warps per CTA")
     args = p.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_gme_batch(args)
     else:
         run_gme(args)
 

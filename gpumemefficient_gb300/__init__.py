@@ -97,6 +97,9 @@ def _declare(L):
                                          _vp, _vp]
     L.gme_batch_stats.argtypes = [_vp, c.POINTER(c.c_int64), c.POINTER(c.c_int64),
                                   c.POINTER(c.c_int64)]
+    L.gme_batch_plan_create.argtypes = [_vp, _vp, c.c_int64, c.c_int64, c.POINTER(c.c_void_p)]
+    L.gme_batch_plan_run.argtypes = [_vp, _vp, c.POINTER(Scoring), _vp, _vp, c.c_int]
+    L.gme_batch_plan_destroy.argtypes = [_vp]
     L.gme_debug_wait_timeout.argtypes = [_vp, c.c_uint64, c.POINTER(c.c_int32)]
     L.gme_launch_count.argtypes = [_vp]
     L.gme_launch_count.restype = c.c_int64
@@ -243,6 +246,35 @@ class Context:
         ks = ctypes.c_int32(-1)
         _check(lib().gme_debug_wait_timeout(self.handle, timeout_ns, ctypes.byref(ks)), self.handle)
         return int(ks.value)
+
+
+class BatchPlan:
+    """A planned batch (fixed pair list) that can be run many times, optionally as a CUDA graph."""
+
+    def __init__(self, ctx: "Context", pairs: np.ndarray, nsym: int):
+        self.ctx = ctx
+        self.pairs = np.ascontiguousarray(pairs, PAIR_DTYPE)
+        h = ctypes.c_void_p()
+        _check(lib().gme_batch_plan_create(ctx.handle, self.pairs.ctypes.data, len(self.pairs), nsym,
+                                           ctypes.byref(h)), ctx.handle)
+        self.handle = h
+
+    def run(self, d_symbols: int, d_results: int, sc: Optional[Scoring] = None, stream: int = 0,
+            use_graph: bool = False):
+        sc = sc or scoring()
+        _check(lib().gme_batch_plan_run(self.handle, d_symbols, ctypes.byref(sc), d_results,
+                                        stream or None, int(use_graph)), self.ctx.handle)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().gme_batch_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def pack_batch(kinds, seqs_a, seqs_b):

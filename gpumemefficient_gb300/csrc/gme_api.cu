@@ -464,6 +464,113 @@ gme_status gme_align_batch(gme_context *ctx, const int32_t *symbols, int64_t nsy
   return GME_OK;
 }
 
+struct gme_batch_plan {
+  gme_context *ctx = nullptr;
+  gme::BatchArena ar;
+  int64_t npairs = 0;
+  int64_t max_len_sum = 0;
+  cudaGraphExec_t exec = nullptr;  // captured launch sequence and what it was captured for
+  const void *g_sym = nullptr;
+  void *g_res = nullptr;
+  cudaStream_t g_st = nullptr;
+  gme_scoring g_sc{};
+  int kernels = 0;
+};
+
+gme_status gme_batch_plan_create(gme_context *ctx, const gme_pair *pairs, int64_t npairs,
+                                 int64_t nsym, gme_batch_plan **out) {
+  if (!ctx || !out || npairs < 0 || nsym < 0 || (npairs > 0 && !pairs)) return GME_ERR_INVALID;
+  *out = nullptr;
+  gme_scoring def = gme_default_scoring();
+  int64_t mx = 0;
+  for (int64_t i = 0; i < npairs; ++i) {
+    gme_status s = check_sizes(ctx, (gme_kind)pairs[i].kind, pairs[i].n1, pairs[i].n2, &def);
+    if (s != GME_OK) {
+      ctx->ws.last_error = "pair " + std::to_string(i) + ": " + ctx->ws.last_error;
+      return s;
+    }
+    mx = std::max<int64_t>(mx, (int64_t)pairs[i].n1 + pairs[i].n2);
+  }
+  cudaSetDevice(ctx->device);
+  gme_batch_plan *p = new (std::nothrow) gme_batch_plan();
+  if (!p) return GME_ERR_NOMEM;
+  p->ctx = ctx;
+  p->npairs = npairs;
+  p->max_len_sum = mx;
+  int rc = gme::batch_plan(ctx->ws, p->ar, pairs, npairs, nsym, ctx->batch_tune, ctx->stream);
+  if (rc != ST_OK) {
+    p->ar.release();
+    delete p;
+    return to_status(rc);
+  }
+  *out = p;
+  return GME_OK;
+}
+
+gme_status gme_batch_plan_run(gme_batch_plan *p, const int32_t *d_symbols, const gme_scoring *sc,
+                              gme_result *d_results, void *stream, int use_graph) {
+  if (!p || (p->npairs > 0 && (!d_symbols || !d_results))) return GME_ERR_INVALID;
+  gme_context *ctx = p->ctx;
+  gme_scoring def = gme_default_scoring();
+  if (!sc) sc = &def;
+  if (sc->ed_boundary != GME_ED_REF_CPU && sc->ed_boundary != GME_ED_STANDARD) return GME_ERR_INVALID;
+  const long long m = std::max<long long>(std::max<long long>(llabs(sc->match), llabs(sc->mismatch)), llabs(sc->gap));
+  if (m * (p->max_len_sum + 2) >= (1ll << 30)) {
+    ctx->ws.last_error = "SW scores could overflow int32";
+    return GME_ERR_OVERFLOW;
+  }
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  const gme::Scoring gs = to_scoring(sc);
+  cudaError_t e;
+  int rc;
+  if (!use_graph) {
+    int k = 0;
+    rc = gme::batch_launch(ctx->ws, p->ar, d_symbols, gs, d_results, st, ctx->timeout_ns, &k);
+    ctx->ws.launches += k;
+    if (rc != ST_OK) return to_status(rc);
+  } else {
+    const bool same = p->exec && p->g_sym == d_symbols && p->g_res == d_results && p->g_st == st &&
+                      memcmp(&p->g_sc, sc, sizeof(gme_scoring)) == 0;
+    if (same) {
+      if ((e = cudaGraphLaunch(p->exec, st)) != cudaSuccess) return to_status(ctx->ws.fail(e, "cudaGraphLaunch"));
+      ctx->ws.launches += p->kernels;
+    } else {
+      if (p->exec) { cudaGraphExecDestroy(p->exec); p->exec = nullptr; }
+      // this run executes uncaptured; the capture is for the next ones
+      int k = 0;
+      rc = gme::batch_launch(ctx->ws, p->ar, d_symbols, gs, d_results, st, ctx->timeout_ns, &k);
+      ctx->ws.launches += k;
+      if (rc != ST_OK) return to_status(rc);
+      cudaGraph_t g = nullptr;
+      if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return to_status(ctx->ws.fail(e, "cudaStreamBeginCapture"));
+      rc = gme::batch_launch(ctx->ws, p->ar, d_symbols, gs, d_results, st, ctx->timeout_ns, &k);
+      e = cudaStreamEndCapture(st, &g);
+      if (rc != ST_OK) { if (g) cudaGraphDestroy(g); return to_status(rc); }
+      if (e != cudaSuccess) return to_status(ctx->ws.fail(e, "cudaStreamEndCapture"));
+      e = cudaGraphInstantiate(&p->exec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) { p->exec = nullptr; return to_status(ctx->ws.fail(e, "cudaGraphInstantiate")); }
+      p->kernels = k;
+      p->g_sym = d_symbols; p->g_res = d_results; p->g_st = st; p->g_sc = *sc;
+    }
+  }
+  struct { gme_context *ctx; const gme_scoring *sc; cudaStream_t st; } arg = {ctx, sc, st};
+  return to_status(gme::batch_long(p->ar, d_symbols, d_results, batch_plain_cb, &arg));
+}
+
+gme_status gme_batch_plan_destroy(gme_batch_plan *p) {
+  if (!p) return GME_ERR_INVALID;
+  cudaSetDevice(p->ctx->device);
+  cudaStreamSynchronize(p->ctx->stream);
+  if (p->g_st) cudaStreamSynchronize(p->g_st);
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  p->ar.release();
+  delete p;
+  return GME_OK;
+}
+
 gme_status gme_batch_stats(const gme_context *ctx, int64_t *block_jobs, int64_t *warp_jobs,
                            int64_t *long_jobs) {
   if (!ctx) return GME_ERR_INVALID;

@@ -425,10 +425,8 @@ __global__ void batch_stage_kernel(const int *__restrict__ src, const long long 
 // ---------------------------------------------------------------------------
 template <int R, int NW>
 static cudaError_t launch_batch_t(const BatchParams &P, int grid, cudaStream_t st) {
-  const size_t smem = sizeof(BatchSmem<NW>);
-  cudaError_t e = cudaFuncSetAttribute(batch_kernel<R, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  batch_kernel<R, NW><<<grid, NW * 32, smem, st>>>(P);
+  // the dynamic shared-memory limit is raised once, when the plan is made
+  batch_kernel<R, NW><<<grid, NW * 32, sizeof(BatchSmem<NW>), st>>>(P);
   return cudaGetLastError();
 }
 
@@ -459,22 +457,22 @@ int batch_occupancy(int NW) {
 
 bool batch_config_valid(int NW) { return NW == 4 || NW == 8; }
 
-int batch_run(Workspace &ws, BatchArena &ar, const int *d_sym, long long nsym, const gme_pair *pairs,
-              long long npairs, const Scoring &sc, gme_result *d_results, cudaStream_t st,
-              const BatchTuning &tune, unsigned long long timeout_ns,
-              int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *),
-              void *plain_ctx) {
+// The plan: classify the pairs (per warp, per CTA, or plain path), order them
+// longest first, lay the staged symbols out and upload the descriptors.  Waits
+// for the arena's previous work on `st` before reusing its buffers.
+int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long npairs,
+               long long nsym, const BatchTuning &tune, cudaStream_t st) {
   constexpr int R = 4;
   const int NW = tune.warps_per_block;
   if (!batch_config_valid(NW)) return ws.fail_msg(ST_INVALID, "batch: warps_per_block must be 4 or 8");
-  // classify
-  std::vector<int> blockj, warpj, longj;
+  std::vector<int> blockj, warpj;
+  ar.longj.clear();
   for (long long i = 0; i < npairs; ++i) {
     const gme_pair &p = pairs[i];
     if (p.n1 < 0 || p.n2 < 0 || p.kind < 0 || p.kind > 2 || p.a_off < 0 || p.b_off < 0 ||
         p.a_off + p.n1 > nsym || p.b_off + p.n2 > nsym)
       return ws.fail_msg(ST_INVALID, "batch: pair " + std::to_string(i) + " out of range");
-    if (p.n1 == 0 || p.n2 == 0 || p.n1 > BLOCK_MAXN) longj.push_back((int)i);
+    if (p.n1 == 0 || p.n2 == 0 || p.n1 > BLOCK_MAXN) ar.longj.push_back((int)i);
     else if (p.n1 <= WARP_MAXN && p.n1 <= tune.warp_max_cols && p.n2 <= tune.warp_max_rows) warpj.push_back((int)i);
     else blockj.push_back((int)i);
   }
@@ -484,6 +482,8 @@ int batch_run(Workspace &ws, BatchArena &ar, const int *d_sym, long long nsym, c
   };
   std::sort(blockj.begin(), blockj.end(), by_cells);
   std::sort(warpj.begin(), warpj.end(), by_cells);
+  ar.long_pairs.clear();
+  for (int i : ar.longj) ar.long_pairs.push_back(pairs[i]);
   // staged layout: a padded with PADL/PADR at a 16-byte aligned start, b padded to whole bands
   const long long nseg = 2 * (long long)(blockj.size() + warpj.size());
   ar.h_from.resize(nseg); ar.h_to.resize(nseg); ar.h_len.resize(nseg); ar.h_padl.resize(nseg); ar.h_total.resize(nseg);
@@ -502,57 +502,94 @@ int batch_run(Workspace &ws, BatchArena &ar, const int *d_sym, long long nsym, c
     j.a_off = place(p.a_off, p.n1, PADL, PADL + p.n1 + PADR);
     const int brows = (p.n2 + rows_mult - 1) / rows_mult * rows_mult;
     j.b_off = place(p.b_off, p.n2, 0, brows);
-    j.n1 = p.n1; j.n2 = p.n2; j.kind = p.kind; j.index = i;
+    j.n1 = p.n1; j.n2 = p.n2; j.kind = p.kind; j.index = (int)i;
     ar.h_jobs[slot] = j;
   };
   size_t slot = 0;
   for (int i : blockj) add(i, 32 * R * NW, slot++);
   for (int i : warpj) add(i, 32 * R, slot++);
-  const long long staged = off + 64;
-  int rc = ar.reserve(staged, nseg, (long long)ar.h_jobs.size(), ws);
-  if (rc != ST_OK) return rc;
   cudaError_t e;
+  if (ar.sync_before_reuse && (e = cudaStreamSynchronize(st)) != cudaSuccess)
+    return ws.fail(e, "cudaStreamSynchronize(batch arena)");
+  int rc = ar.reserve(off + 64, nseg, (long long)ar.h_jobs.size(), ws);
+  if (rc != ST_OK) return rc;
   if (nseg > 0) {
-    if ((e = cudaMemcpyAsync(ar.d_from, ar.h_from.data(), nseg * 8, cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(ar.d_to, ar.h_to.data(), nseg * 8, cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(ar.d_len, ar.h_len.data(), nseg * 4, cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(ar.d_padl, ar.h_padl.data(), nseg * 4, cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(ar.d_total, ar.h_total.data(), nseg * 4, cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(ar.d_jobs, ar.h_jobs.data(), ar.h_jobs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice, st)))
-      return ws.fail(e, "cudaMemcpyAsync(batch plan)");
-    // the host vectors must outlive the copies
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return ws.fail(e, "cudaStreamSynchronize(batch plan)");
-    const int blocks = (int)std::min<long long>(nseg, 65535);
-    batch_stage_kernel<<<blocks, 256, 0, st>>>(d_sym, ar.d_from, ar.d_to, ar.d_len, ar.d_padl, ar.d_total, (int)nseg, ar.d_staged);
-    ws.launches += 1;
-    if ((e = cudaGetLastError()) != cudaSuccess) return ws.fail(e, "batch_stage_kernel");
-    if ((e = cudaMemsetAsync(ar.d_ctrl, 0, 4 * sizeof(int), st)) != cudaSuccess) return ws.fail(e, "cudaMemsetAsync(batch ctrl)");
-    BatchParams P;
-    P.sym = ar.d_staged;
-    P.jobs_b = reinterpret_cast<const BatchJob *>(ar.d_jobs);
-    P.jobs_w = P.jobs_b + blockj.size();
-    P.n_b = (int)blockj.size();
-    P.n_w = (int)warpj.size();
-    P.results = d_results;
-    P.ctrl = ar.d_ctrl;
-    P.sc = sc;
-    P.timeout_ns = timeout_ns;
-    int occ = batch_occupancy(NW);
-    if (occ < 1) occ = 1;
-    int grid = ws.sms * std::min(occ, tune.blocks_per_sm > 0 ? tune.blocks_per_sm : occ);
-    if ((e = launch_batch(NW, P, grid, st)) != cudaSuccess) return ws.fail(e, "batch_kernel");
-    ws.launches += 1;
+    if ((e = cudaMemcpy(ar.d_from, ar.h_from.data(), nseg * 8, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(ar.d_to, ar.h_to.data(), nseg * 8, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(ar.d_len, ar.h_len.data(), nseg * 4, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(ar.d_padl, ar.h_padl.data(), nseg * 4, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(ar.d_total, ar.h_total.data(), nseg * 4, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(ar.d_jobs, ar.h_jobs.data(), ar.h_jobs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice)))
+      return ws.fail(e, "cudaMemcpy(batch plan)");
   }
-  // pairs the shared-memory rows cannot hold: the plain path, one launch each
-  for (int i : longj) {
-    const gme_pair &p = pairs[i];
-    rc = plain(plain_ctx, p.kind, d_sym + p.a_off, p.n1, d_sym + p.b_off, p.n2, d_results + i);
+  ar.nseg = nseg;
+  ar.n_b = (int)blockj.size();
+  ar.n_w = (int)warpj.size();
+  ar.NW = NW;
+  int occ = batch_occupancy(NW);
+  if (occ < 1) occ = 1;
+  ar.grid = ws.sms * std::min(occ, tune.blocks_per_sm > 0 ? tune.blocks_per_sm : occ);
+  ar.last_block_jobs = ar.n_b;
+  ar.last_warp_jobs = ar.n_w;
+  ar.last_long_jobs = (long long)ar.longj.size();
+  return ST_OK;
+}
+
+// The launches of a planned batch: clear the tickets, stage the symbols, run the
+// work-queue kernel.  Stream operations only, so the sequence can be captured.
+// Returns the number of kernels launched in *kernels.
+int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring &sc,
+                 gme_result *d_results, cudaStream_t st, unsigned long long timeout_ns, int *kernels) {
+  *kernels = 0;
+  if (ar.nseg == 0) return ST_OK;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(ar.d_ctrl, 0, 4 * sizeof(int), st)) != cudaSuccess)
+    return ws.fail(e, "cudaMemsetAsync(batch ctrl)");
+  const int blocks = (int)std::min<long long>(ar.nseg, 65535);
+  batch_stage_kernel<<<blocks, 256, 0, st>>>(d_sym, ar.d_from, ar.d_to, ar.d_len, ar.d_padl,
+                                             ar.d_total, (int)ar.nseg, ar.d_staged);
+  if ((e = cudaGetLastError()) != cudaSuccess) return ws.fail(e, "batch_stage_kernel");
+  BatchParams P;
+  P.sym = ar.d_staged;
+  P.jobs_b = ar.d_jobs;
+  P.jobs_w = ar.d_jobs + ar.n_b;
+  P.n_b = ar.n_b;
+  P.n_w = ar.n_w;
+  P.results = d_results;
+  P.ctrl = ar.d_ctrl;
+  P.sc = sc;
+  P.timeout_ns = timeout_ns;
+  if ((e = launch_batch(ar.NW, P, ar.grid, st)) != cudaSuccess) return ws.fail(e, "batch_kernel");
+  *kernels = 2;
+  return ST_OK;
+}
+
+// Pairs the shared-memory rows cannot hold (or empty ones): the plain path, one
+// call each.  Never captured: the plain path hands out fresh band tags per call.
+int batch_long(BatchArena &ar, const int *d_sym, gme_result *d_results,
+               int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *),
+               void *plain_ctx) {
+  for (size_t k = 0; k < ar.longj.size(); ++k) {
+    const gme_pair &p = ar.long_pairs[k];
+    const int rc = plain(plain_ctx, p.kind, d_sym + p.a_off, p.n1, d_sym + p.b_off, p.n2,
+                         d_results + ar.longj[k]);
     if (rc != ST_OK) return rc;
   }
-  ar.last_block_jobs = (long long)blockj.size();
-  ar.last_warp_jobs = (long long)warpj.size();
-  ar.last_long_jobs = (long long)longj.size();
   return ST_OK;
+}
+
+int batch_run(Workspace &ws, BatchArena &ar, const int *d_sym, long long nsym, const gme_pair *pairs,
+              long long npairs, const Scoring &sc, gme_result *d_results, cudaStream_t st,
+              const BatchTuning &tune, unsigned long long timeout_ns,
+              int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *),
+              void *plain_ctx) {
+  int rc = batch_plan(ws, ar, pairs, npairs, nsym, tune, st);
+  if (rc != ST_OK) return rc;
+  int k = 0;
+  rc = batch_launch(ws, ar, d_sym, sc, d_results, st, timeout_ns, &k);
+  ws.launches += k;
+  if (rc != ST_OK) return rc;
+  return batch_long(ar, d_sym, d_results, plain, plain_ctx);
 }
 
 }  // namespace gme

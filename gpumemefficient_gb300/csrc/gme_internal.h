@@ -65,6 +65,12 @@ struct BatchArena {
   BatchJob *d_jobs = nullptr; long long jobs_cap = 0;
   int *d_ctrl = nullptr;
   long long last_block_jobs = 0, last_warp_jobs = 0, last_long_jobs = 0;
+  // the plan
+  long long nseg = 0;
+  int n_b = 0, n_w = 0, NW = 4, grid = 0;
+  std::vector<int> longj;             // result slots of pairs for the plain path
+  std::vector<gme_pair> long_pairs;   // their descriptors
+  bool sync_before_reuse = true;      // wait for the stream before overwriting the plan
   int reserve(long long staged, long long nseg, long long njobs, Workspace &ws);
   void release();
 };
@@ -72,6 +78,13 @@ struct BatchArena {
 // batched path (gme_batch.cu)
 bool batch_config_valid(int NW);
 int batch_occupancy(int NW);
+int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long npairs,
+               long long nsym, const BatchTuning &tune, cudaStream_t st);
+int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring &sc,
+                 gme_result *d_results, cudaStream_t st, unsigned long long timeout_ns, int *kernels);
+int batch_long(BatchArena &ar, const int *d_sym, gme_result *d_results,
+               int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *),
+               void *plain_ctx);
 int batch_run(Workspace &ws, BatchArena &ar, const int *d_sym, long long nsym, const gme_pair *pairs,
               long long npairs, const Scoring &sc, gme_result *d_results, cudaStream_t st,
               const BatchTuning &tune, unsigned long long timeout_ns,

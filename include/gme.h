@@ -147,6 +147,21 @@ gme_status gme_align_batch(gme_context *ctx, const int32_t *symbols, int64_t nsy
 gme_status gme_align_batch_device(gme_context *ctx, const int32_t *d_symbols, int64_t nsym,
                                   const gme_pair *pairs, int64_t npairs, const gme_scoring *sc,
                                   gme_result *d_results, void *stream);
+/* A reusable plan for a fixed pair list: classification, ordering, staged layout
+ * and descriptors are made once; each run only clears the tickets, stages the
+ * symbols and launches the work-queue kernel.  With use_graph != 0 the first run
+ * also captures that launch sequence into a CUDA graph, and later runs with the
+ * same symbol/result pointers, stream and scoring replay the graph (one launch
+ * from the host).  Pairs the batch hands to the plain path run outside the graph.
+ * A plan belongs to its context's thread; runs of one plan must not overlap. */
+typedef struct gme_batch_plan gme_batch_plan;
+gme_status gme_batch_plan_create(gme_context *ctx, const gme_pair *pairs, int64_t npairs,
+                                 int64_t nsym, gme_batch_plan **plan);
+gme_status gme_batch_plan_run(gme_batch_plan *plan, const int32_t *d_symbols,
+                              const gme_scoring *sc, gme_result *d_results, void *stream,
+                              int use_graph);
+gme_status gme_batch_plan_destroy(gme_batch_plan *plan);
+
 /* How the last batch was split: one-per-CTA, one-per-warp and plain-path pairs. */
 gme_status gme_batch_stats(const gme_context *ctx, int64_t *block_jobs, int64_t *warp_jobs,
                            int64_t *long_jobs);

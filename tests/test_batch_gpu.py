@@ -87,3 +87,32 @@ def test_warp_cutoffs(gme_ctx):
             check_batch(gme_ctx, kinds, sa, sb)
         finally:
             gme_ctx.set_batch_config()
+
+
+def test_plan_graph_replay(gme_ctx):
+    """A planned batch run three times: uncaptured, first graph run (captures), replay."""
+    import torch
+    import gpumemefficient_gb300 as g
+    rng = np.random.default_rng(21)
+    n = 300
+    kinds = rng.integers(0, 3, n)
+    sa = [rng.integers(0, 4, k) for k in np.exp(rng.uniform(0, np.log(2500), n)).astype(int)]
+    sb = [rng.integers(0, 4, k) for k in np.exp(rng.uniform(0, np.log(2500), n)).astype(int)]
+    sa[3] = rng.integers(0, 4, 5000)  # one pair for the plain path (n1 > 4096)
+    symbols, pairs = g.pack_batch(kinds, sa, sb)
+    o = O.align_batch(kinds, sa, sb)
+    dev = torch.device("cuda", 0)
+    d_sym = torch.from_numpy(symbols).to(dev)
+    d_res = torch.zeros(n * g.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    plan = g.BatchPlan(gme_ctx, pairs, len(symbols))
+    try:
+        for use_graph in (False, True, True, True):
+            d_res.zero_()
+            torch.cuda.synchronize()
+            plan.run(d_sym.data_ptr(), d_res.data_ptr(), use_graph=use_graph)
+            torch.cuda.synchronize()
+            res = np.frombuffer(d_res.cpu().numpy().tobytes(), g.RESULT_DTYPE)
+            np.testing.assert_array_equal(res["status"], 0)
+            np.testing.assert_array_equal(res["score"], o["score"])
+    finally:
+        plan.close()
