@@ -180,6 +180,7 @@ __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict_
 #pragma unroll
   for (int k = C; k < 2 * C - R; ++k) win[k] = 0;
 
+  const int row_end = ((N + 1 + C - 1) / C) * C;  // ring positions carrying this row
   int recv = 0, recv_prev = 0;
   int ib[2][C];
   int tag_next = src_tag<KIND>(in, 0);
@@ -196,7 +197,9 @@ __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict_
       if (!W.wait(ready)) return false;
       src_load<KIND>(in, j, inv);
     }
-    if (in.mode == IN_RING && lane == 31) sts_vol(in.cons, in.base + s0 + C);
+    // consumed: this chunk, but never past the end of this band's row -- the ring's
+    // next positions already belong to the next band group of the same pair
+    if (in.mode == IN_RING && lane == 31) sts_vol(in.cons, in.base + min(s0 + C, row_end));
     if (lane == 0) recv = inv[0];
     tag_next = src_tag<KIND>(in, j + 1);
     src_load<KIND>(in, j + 1, ib[PAR ^ 1]);
