@@ -503,6 +503,9 @@ gme_status gme_batch_plan_create(gme_context *ctx, const gme_pair *pairs, int64_
     delete p;
     return to_status(rc);
   }
+  ctx->batch.last_block_jobs = p->ar.last_block_jobs;
+  ctx->batch.last_warp_jobs = p->ar.last_warp_jobs;
+  ctx->batch.last_long_jobs = p->ar.last_long_jobs;
   *out = p;
   return GME_OK;
 }

@@ -228,15 +228,18 @@ __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict_
     if (j <= jb && !chunk(j, P0{}, ck, pd)) return false;
     return true;
   };
+  // Two chunk bodies per parity keep the code small (the instruction cache is
+  // shared by every kind in flight on an SM): the steady one, and one that both
+  // holds out-of-range cells and passes padding rows through (ramps, last band).
   const int j_end = (N + 32 * R) / C;
   if (padwarp) {
     if (!range(0, j_end, T{}, T{})) return false;
   } else {
     const int j_lo = min((32 * R) / C, j_end + 1);
     const int j_hi = max(min((N - C + 1) / C, j_end), j_lo - 1);
-    if (!range(0, j_lo - 1, T{}, F{})) return false;
+    if (!range(0, j_lo - 1, T{}, T{})) return false;
     if (!range(j_lo, j_hi, F{}, F{})) return false;
-    if (!range(j_hi + 1, j_end, T{}, F{})) return false;
+    if (!range(j_hi + 1, j_end, T{}, T{})) return false;
   }
   corner = cur[R - 1];
 #pragma unroll
@@ -479,7 +482,9 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
     else if (p.n1 <= WARP_MAXN && p.n1 <= tune.warp_max_cols && p.n2 <= tune.warp_max_rows) warpj.push_back((int)i);
     else blockj.push_back((int)i);
   }
+  // one kind after another (an SM then runs one kind's code at a time), longest first
   auto by_cells = [&](int x, int y) {
+    if (pairs[x].kind != pairs[y].kind) return pairs[x].kind < pairs[y].kind;
     const long long cx = (long long)pairs[x].n1 * pairs[x].n2, cy = (long long)pairs[y].n1 * pairs[y].n2;
     return cx != cy ? cx > cy : x < y;
   };

@@ -162,7 +162,7 @@ gme_status gme_batch_plan_run(gme_batch_plan *plan, const int32_t *d_symbols,
                               int use_graph);
 gme_status gme_batch_plan_destroy(gme_batch_plan *plan);
 
-/* How the last batch was split: one-per-CTA, one-per-warp and plain-path pairs. */
+/* How the last batch (or last plan made) was split: one-per-CTA, one-per-warp and plain-path pairs. */
 gme_status gme_batch_stats(const gme_context *ctx, int64_t *block_jobs, int64_t *warp_jobs,
                            int64_t *long_jobs);
 
