@@ -56,7 +56,7 @@ class Pair(ctypes.Structure):
 
 class BatchConfig(ctypes.Structure):
     _fields_ = [("warps_per_block", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
-                ("warp_max_rows", ctypes.c_int32), ("warp_max_cols", ctypes.c_int32)]
+                ("block_min_cells", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 PAIR_DTYPE = np.dtype([("a_off", "<i8"), ("b_off", "<i8"), ("n1", "<i4"), ("n2", "<i4"),
@@ -213,8 +213,8 @@ class Context:
                                       stream or None), self.handle)
 
     def set_batch_config(self, warps_per_block: int = 0, blocks_per_sm: int = 0,
-                         warp_max_rows: int = 0, warp_max_cols: int = 0):
-        cfg = BatchConfig(warps_per_block, blocks_per_sm, warp_max_rows, warp_max_cols)
+                         block_min_cells: int = 0):
+        cfg = BatchConfig(warps_per_block, blocks_per_sm, block_min_cells, 0)
         _check(lib().gme_set_batch_config(self.handle, ctypes.byref(cfg)), self.handle)
 
     def batch_stats(self) -> dict:

@@ -95,7 +95,14 @@ int BatchArena::reserve(long long staged, long long nseg, long long njobs, Works
   return ST_OK;
 }
 
+int BatchArena::reserve_rows(long long ints, Workspace &ws) {
+  return grow_ll((void **)&d_rows, &rows_cap, ints, sizeof(int), ws, "cudaMalloc(batch rows)");
+}
+
 void BatchArena::release() {
+  cudaFree(d_rows);
+  d_rows = nullptr;
+  rows_cap = 0;
   cudaFree(d_staged); cudaFree(d_from); cudaFree(d_to); cudaFree(d_len); cudaFree(d_padl);
   cudaFree(d_total); cudaFree(d_jobs); cudaFree(d_ctrl);
   d_staged = nullptr; d_from = d_to = nullptr; d_len = d_padl = d_total = nullptr; d_jobs = nullptr;
@@ -399,12 +406,9 @@ gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg) {
       }
       t.warps_per_block = cfg->warps_per_block;
     }
-    if (cfg->blocks_per_sm < 0 || cfg->warp_max_rows < 0 || cfg->warp_max_cols < 0 ||
-        cfg->warp_max_cols > 1024)
-      return GME_ERR_INVALID;
+    if (cfg->blocks_per_sm < 0 || cfg->block_min_cells < 0) return GME_ERR_INVALID;
     t.blocks_per_sm = cfg->blocks_per_sm;
-    if (cfg->warp_max_rows) t.warp_max_rows = cfg->warp_max_rows;
-    if (cfg->warp_max_cols) t.warp_max_cols = cfg->warp_max_cols;
+    if (cfg->block_min_cells) t.block_min_cells = cfg->block_min_cells;
   }
   ctx->batch_tune = t;
   return GME_OK;

@@ -23,12 +23,11 @@
 
 namespace gme {
 
-constexpr int BLOCK_MAXN = 4096;  // widest pair (n1) a block job keeps in shared memory
-constexpr int WARP_MAXN = 1024;   // widest pair a warp job keeps in shared memory
+constexpr int BLOCK_MAXN = 4096;  // widest pair (n1) the batch kernel takes (rows in shared or L2)
 // a row is read up to one chunk past the last chunk (the read-ahead): j_end+1 with
 // j_end = (n1 + 32R)/C, so a row of n1 columns needs n1 + 32R + 2C entries (R <= 8)
 constexpr int ROWSTRIDE_B = BLOCK_MAXN + 32 * 8 + 3 * C;
-constexpr int ROWSTRIDE_W = WARP_MAXN + 32 * 8 + 3 * C;
+constexpr int ROWSTRIDE_G = BLOCK_MAXN + 32 * 8 + 3 * C;  // a warp job's row in global memory
 
 struct BatchParams {
   const int *sym;          // staged, padded symbols
@@ -36,6 +35,7 @@ struct BatchParams {
   const BatchJob *jobs_w;  // warp jobs, longest first
   int n_b, n_w;
   gme_result *results;
+  int *rows;  // warp jobs: one row of ROWSTRIDE_G ints per warp of the grid (L2-resident)
   int *ctrl;  // [0] block ticket, [1] warp ticket, [2] status
   Scoring sc;
   unsigned long long timeout_ns;
@@ -50,7 +50,6 @@ template <int NW> struct __align__(16) BatchSmem {
       int row[2][ROWSTRIDE_B];  // warp NW-1 -> warp 0 across band groups
       int tag[2][ROWSTRIDE_B / C];
     } wrap;
-    int own[NW][ROWSTRIDE_W];  // warp jobs: each warp's own row
   } u;
   int job;
   int abort;
@@ -102,6 +101,16 @@ __device__ __forceinline__ void src_load(const Src &s, int j, int (&d)[C]) {
     return;
   }
   const int *p = (s.mode == IN_RING) ? s.buf + ((s.base + C * j) & (RING - 1)) : s.buf + C * j;
+  if (s.mode == IN_OWN) {
+    // the warp's own row in global memory, written by lane 31 one band earlier:
+    // read at L2 (.cg) so that no lane sees a line its L1 kept from before the write
+#pragma unroll
+    for (int k = 0; k < C; k += 4) {
+      const int4 q = __ldcg(reinterpret_cast<const int4 *>(p + k));
+      d[k] = q.x; d[k + 1] = q.y; d[k + 2] = q.z; d[k + 3] = q.w;
+    }
+    return;
+  }
 #pragma unroll
   for (int k = 0; k < C; k += 4) {
     const int4 q = *reinterpret_cast<const int4 *>(p + k);
@@ -338,7 +347,7 @@ __device__ void warp_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob 
   const int *a_sym = P.sym + jb.a_off;
   const int *b_sym = P.sym + jb.b_off;
   const int nb = (M + 32 * R - 1) / (32 * R);
-  int *row = S.u.own[warp];
+  int *row = P.rows + ((long long)blockIdx.x * NW + warp) * ROWSTRIDE_G;
   SwBest tb = {0, 0, 0, 0};
   int corner = 0;
   for (int band = 0; band < nb; ++band) {
@@ -479,8 +488,8 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
         p.a_off + p.n1 > nsym || p.b_off + p.n2 > nsym)
       return ws.fail_msg(ST_INVALID, "batch: pair " + std::to_string(i) + " out of range");
     if (p.n1 == 0 || p.n2 == 0 || p.n1 > BLOCK_MAXN) ar.longj.push_back((int)i);
-    else if (p.n1 <= WARP_MAXN && p.n1 <= tune.warp_max_cols && p.n2 <= tune.warp_max_rows) warpj.push_back((int)i);
-    else blockj.push_back((int)i);
+    else if ((long long)p.n1 * p.n2 >= tune.block_min_cells && p.n2 > 32 * R * (NW - 1)) blockj.push_back((int)i);
+    else warpj.push_back((int)i);
   }
   // one kind after another (an SM then runs one kind's code at a time), longest first
   auto by_cells = [&](int x, int y) {
@@ -521,6 +530,10 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
     return ws.fail(e, "cudaStreamSynchronize(batch arena)");
   int rc = ar.reserve(off + 64, nseg, (long long)ar.h_jobs.size(), ws);
   if (rc != ST_OK) return rc;
+  int occ0 = batch_occupancy(NW);
+  if (occ0 < 1) occ0 = 1;
+  const int grid0 = ws.sms * std::min(occ0, tune.blocks_per_sm > 0 ? tune.blocks_per_sm : occ0);
+  if ((rc = ar.reserve_rows((long long)grid0 * NW * ROWSTRIDE_G, ws)) != ST_OK) return rc;
   if (nseg > 0) {
     if ((e = cudaMemcpy(ar.d_from, ar.h_from.data(), nseg * 8, cudaMemcpyHostToDevice)) ||
         (e = cudaMemcpy(ar.d_to, ar.h_to.data(), nseg * 8, cudaMemcpyHostToDevice)) ||
@@ -564,6 +577,7 @@ int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring 
   P.n_b = ar.n_b;
   P.n_w = ar.n_w;
   P.results = d_results;
+  P.rows = ar.d_rows;
   P.ctrl = ar.d_ctrl;
   P.sc = sc;
   P.timeout_ns = timeout_ns;

@@ -50,8 +50,8 @@ struct BatchJob {
 struct BatchTuning {
   int warps_per_block = 4;  // compute warps of a CTA (block jobs pipeline them over bands)
   int blocks_per_sm = 0;    // 0 = as many as fit
-  int warp_max_rows = 512;  // pairs up to this many rows (and up to 1024 columns) run one per warp
-  int warp_max_cols = 1024;
+  long long block_min_cells = 1ll << 22;  // pairs at least this large (and with a band per warp) run one per CTA
+
 };
 
 // Device and host buffers of the batched path, owned by a context, grown on demand.
@@ -64,6 +64,7 @@ struct BatchArena {
   int *d_len = nullptr, *d_padl = nullptr, *d_total = nullptr; long long seg_cap = 0;
   BatchJob *d_jobs = nullptr; long long jobs_cap = 0;
   int *d_ctrl = nullptr;
+  int *d_rows = nullptr; long long rows_cap = 0;  // warp jobs' rows
   long long last_block_jobs = 0, last_warp_jobs = 0, last_long_jobs = 0;
   // the plan
   long long nseg = 0;
@@ -72,6 +73,7 @@ struct BatchArena {
   std::vector<gme_pair> long_pairs;   // their descriptors
   bool sync_before_reuse = true;      // wait for the stream before overwriting the plan
   int reserve(long long staged, long long nseg, long long njobs, Workspace &ws);
+  int reserve_rows(long long ints, Workspace &ws);
   void release();
 };
 

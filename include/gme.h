@@ -117,9 +117,10 @@ gme_status gme_align_device(gme_context *ctx, gme_kind kind, const int32_t *d_a,
 /* ---- batched path: many alignments in one launch --------------------------------
  * Pair i reads a = symbols[a_off .. a_off+n1), b = symbols[b_off .. b_off+n2) and
  * computes `kind` with the shared scoring; result i gets its score (and SW maximum).
- * One persistent work-queue kernel runs every pair whose n1 <= 4096: pairs with
- * n2 <= warp_max_rows and n1 <= warp_max_cols one per warp, the rest one per CTA
- * (the CTA's warps pipelined over the pair's bands), longest first.  Wider or empty
+ * One persistent work-queue kernel runs every pair whose n1 <= 4096: pairs of at
+ * least block_min_cells cells (and at least one band of 128 rows per warp) one per
+ * CTA (the CTA's warps pipelined over the pair's bands), all others one per warp;
+ * kinds one after another, longest first.  Wider or empty
  * pairs run on the plain path, one launch each, on the same stream.  Replaces calling
  * the reference's one-pair host function (e.g. EditDistance/GPU_Hyperlane_Share.cu:689)
  * once per pair. */
@@ -133,8 +134,8 @@ typedef struct gme_pair {
 typedef struct gme_batch_config {
   int32_t warps_per_block; /* 4 or 8 (0 = automatic) */
   int32_t blocks_per_sm;   /* CTAs per SM (0 = as many as fit) */
-  int32_t warp_max_rows;   /* pairs with n2 <= this (and n1 <= warp_max_cols) run one per warp */
-  int32_t warp_max_cols;   /* at most 1024 */
+  int32_t block_min_cells; /* pairs with n1*n2 >= this run one per CTA (0 = 2^22) */
+  int32_t reserved;
 } gme_batch_config;
 
 gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg);

@@ -30,7 +30,7 @@ def test_mixed_uneven(gme_ctx, nw):
     lb = np.exp(rng.uniform(np.log(1), np.log(3000), n)).astype(int)
     sa = [rng.integers(0, 4, k) for k in la]
     sb = [rng.integers(0, 4, k) for k in lb]
-    gme_ctx.set_batch_config(warps_per_block=nw)
+    gme_ctx.set_batch_config(warps_per_block=nw, block_min_cells=1 << 18)
     try:
         check_batch(gme_ctx, kinds, sa, sb, rule=0)
         check_batch(gme_ctx, kinds, sa, sb, rule=1)
@@ -76,13 +76,13 @@ def test_batch_sw_scoring(gme_ctx):
     check_batch(gme_ctx, kinds, sa, sb, sc=g.scoring(5, -4, -7))
 
 
-def test_warp_cutoffs(gme_ctx):
+def test_block_cutoffs(gme_ctx):
     rng = np.random.default_rng(12)
     kinds = rng.integers(0, 3, 200)
-    sa = [rng.integers(0, 4, rng.integers(10, 1100)) for _ in kinds]
-    sb = [rng.integers(0, 4, rng.integers(10, 1100)) for _ in kinds]
-    for rows, cols in [(128, 256), (1024, 1024), (4096, 1024)]:
-        gme_ctx.set_batch_config(warp_max_rows=rows, warp_max_cols=cols)
+    sa = [rng.integers(0, 4, rng.integers(10, 2100)) for _ in kinds]
+    sb = [rng.integers(0, 4, rng.integers(10, 2100)) for _ in kinds]
+    for cells in [1, 1 << 16, 1 << 20, 1 << 30]:
+        gme_ctx.set_batch_config(block_min_cells=cells)
         try:
             check_batch(gme_ctx, kinds, sa, sb)
         finally:
