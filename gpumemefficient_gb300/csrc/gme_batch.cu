@@ -23,11 +23,20 @@
 
 namespace gme {
 
+// Wavefront steps per ring transaction in this kernel.  Shorter than the plain
+// kernel's: a dozen independent warps per SM each run their own pair at their own
+// point in the loop, so the loop body must stay small for the instruction cache.
+#ifndef GME_BATCH_CHUNK
+#define GME_BATCH_CHUNK 8
+#endif
+constexpr int CB = GME_BATCH_CHUNK;
+
+
 constexpr int BLOCK_MAXN = 4096;  // widest pair (n1) the batch kernel takes (rows in shared or L2)
 // a row is read up to one chunk past the last chunk (the read-ahead): j_end+1 with
-// j_end = (n1 + 32R)/C, so a row of n1 columns needs n1 + 32R + 2C entries (R <= 8)
-constexpr int ROWSTRIDE_B = BLOCK_MAXN + 32 * 8 + 3 * C;
-constexpr int ROWSTRIDE_G = BLOCK_MAXN + 32 * 8 + 3 * C;  // a warp job's row in global memory
+// j_end = (n1 + 32R)/CB, so a row of n1 columns needs n1 + 32R + 2C entries (R <= 8)
+constexpr int ROWSTRIDE_B = BLOCK_MAXN + 32 * 8 + 3 * CB;
+constexpr int ROWSTRIDE_G = BLOCK_MAXN + 32 * 8 + 3 * CB;  // a warp job's row in global memory
 
 struct BatchParams {
   const int *sym;          // staged, padded symbols
@@ -43,12 +52,12 @@ struct BatchParams {
 
 template <int NW> struct __align__(16) BatchSmem {
   int ring[NW][RING];       // ring[w]: warp w-1 -> warp w (w >= 1)
-  int tag[NW][RING / C];
+  int tag[NW][RING / CB];
   int cons[NW];
   union {
     struct {
       int row[2][ROWSTRIDE_B];  // warp NW-1 -> warp 0 across band groups
-      int tag[2][ROWSTRIDE_B / C];
+      int tag[2][ROWSTRIDE_B / CB];
     } wrap;
   } u;
   int job;
@@ -84,49 +93,49 @@ struct Dst {
 
 template <int KIND>
 __device__ __forceinline__ int src_tag(const Src &s, int j) {
-  if (s.mode == IN_RING) return ld_acquire_cta(&s.tags[(s.base / C + j) & (RING / C - 1)]);
+  if (s.mode == IN_RING) return ld_acquire_cta(&s.tags[(s.base / CB + j) & (RING / CB - 1)]);
   if (s.mode == IN_ROW) return ld_acquire_cta(&s.tags[j]);
   return 0;
 }
 __device__ __forceinline__ int src_want(const Src &s, int j) {
-  if (s.mode == IN_RING) return s.base / C + j + 1;
+  if (s.mode == IN_RING) return s.base / CB + j + 1;
   if (s.mode == IN_ROW) return s.base + j + 1;
   return 0;
 }
 template <int KIND>
-__device__ __forceinline__ void src_load(const Src &s, int j, int (&d)[C]) {
+__device__ __forceinline__ void src_load(const Src &s, int j, int (&d)[CB]) {
   if (s.mode == IN_TOP) {
 #pragma unroll
-    for (int k = 0; k < C; ++k) d[k] = Rec<KIND>::top(C * j + k, s.rule);
+    for (int k = 0; k < CB; ++k) d[k] = Rec<KIND>::top(CB * j + k, s.rule);
     return;
   }
-  const int *p = (s.mode == IN_RING) ? s.buf + ((s.base + C * j) & (RING - 1)) : s.buf + C * j;
+  const int *p = (s.mode == IN_RING) ? s.buf + ((s.base + CB * j) & (RING - 1)) : s.buf + CB * j;
   if (s.mode == IN_OWN) {
     // the warp's own row in global memory, written by lane 31 one band earlier:
     // read at L2 (.cg) so that no lane sees a line its L1 kept from before the write
 #pragma unroll
-    for (int k = 0; k < C; k += 4) {
+    for (int k = 0; k < CB; k += 4) {
       const int4 q = __ldcg(reinterpret_cast<const int4 *>(p + k));
       d[k] = q.x; d[k + 1] = q.y; d[k + 2] = q.z; d[k + 3] = q.w;
     }
     return;
   }
 #pragma unroll
-  for (int k = 0; k < C; k += 4) {
+  for (int k = 0; k < CB; k += 4) {
     const int4 q = *reinterpret_cast<const int4 *>(p + k);
     d[k] = q.x; d[k + 1] = q.y; d[k + 2] = q.z; d[k + 3] = q.w;
   }
 }
 
-__device__ __forceinline__ bool dst_put(Dst &o, int pos, const int (&q)[C], int lane, Waiter &W) {
+__device__ __forceinline__ bool dst_put(Dst &o, int pos, const int (&q)[CB], int lane, Waiter &W) {
   if (o.mode == OUT_NONE) return true;
   int *p;
   if (o.mode == OUT_RING) {
     const int sp = o.base + pos;
-    if (sp + C - RING > o.cons_seen) {
+    if (sp + CB - RING > o.cons_seen) {
       if (!W.wait([&] {
             o.cons_seen = __shfl_sync(FULL, lds_vol(o.cons), 0);
-            return o.cons_seen >= sp + C - RING;
+            return o.cons_seen >= sp + CB - RING;
           }))
         return false;
     }
@@ -136,10 +145,10 @@ __device__ __forceinline__ bool dst_put(Dst &o, int pos, const int (&q)[C], int 
   }
   if (lane == 31) {
 #pragma unroll
-    for (int k = 0; k < C; k += 4)
+    for (int k = 0; k < CB; k += 4)
       *reinterpret_cast<int4 *>(p + k) = make_int4(q[k], q[k + 1], q[k + 2], q[k + 3]);
-    if (o.mode == OUT_RING) st_release_cta(&o.tags[((o.base + pos) / C) & (RING / C - 1)], (o.base + pos) / C + 1);
-    else if (o.mode == OUT_ROW) st_release_cta(&o.tags[pos / C], o.base + pos / C + 1);
+    if (o.mode == OUT_RING) st_release_cta(&o.tags[((o.base + pos) / CB) & (RING / CB - 1)], (o.base + pos) / CB + 1);
+    else if (o.mode == OUT_ROW) st_release_cta(&o.tags[pos / CB], o.base + pos / CB + 1);
   }
   return true;
 }
@@ -174,32 +183,32 @@ __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict_
   const bool padwarp = __any_sync(FULL, padmask != 0);
 
   const int *sym = a_sym + (PADL - 1 - lane * R);
-  int win[2 * C];
+  int win[2 * CB];
 #pragma unroll
-  for (int k = 0; k < C; k += 4) {
+  for (int k = 0; k < CB; k += 4) {
     const int4 q = ldg4(sym + k);
     win[k] = q.x; win[k + 1] = q.y; win[k + 2] = q.z; win[k + 3] = q.w;
   }
 #pragma unroll
   for (int k = 0; k < R; k += 4) {
     const int4 q = ldg4(sym - R + k);
-    win[2 * C - R + k] = q.x; win[2 * C - R + k + 1] = q.y;
-    win[2 * C - R + k + 2] = q.z; win[2 * C - R + k + 3] = q.w;
+    win[2 * CB - R + k] = q.x; win[2 * CB - R + k + 1] = q.y;
+    win[2 * CB - R + k + 2] = q.z; win[2 * CB - R + k + 3] = q.w;
   }
 #pragma unroll
-  for (int k = C; k < 2 * C - R; ++k) win[k] = 0;
+  for (int k = CB; k < 2 * CB - R; ++k) win[k] = 0;
 
-  const int row_end = ((N + 1 + C - 1) / C) * C;  // ring positions carrying this row
+  const int row_end = ((N + 1 + CB - 1) / CB) * CB;  // ring positions carrying this row
   int recv = 0, recv_prev = 0;
-  int ib[2][C];
+  int ib[2][CB];
   int tag_next = src_tag<KIND>(in, 0);
   src_load<KIND>(in, 0, ib[0]);
 
   auto chunk = [&](int j, auto par, auto checked, auto padrows) -> bool {
     constexpr int PAR = decltype(par)::value;
     constexpr bool CK = decltype(checked)::value, PD = decltype(padrows)::value;
-    int(&inv)[C] = ib[PAR];
-    const int s0 = C * j;
+    int(&inv)[CB] = ib[PAR];
+    const int s0 = CB * j;
     __syncwarp();
     if (s0 <= N && !__all_sync(FULL, tag_next == src_want(in, j))) {
       auto ready = [&] { return __all_sync(FULL, src_tag<KIND>(in, j) == src_want(in, j)); };
@@ -208,12 +217,12 @@ __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict_
     }
     // consumed: this chunk, but never past the end of this band's row -- the ring's
     // next positions already belong to the next band group of the same pair
-    if (in.mode == IN_RING && lane == 31) sts_vol(in.cons, in.base + min(s0 + C, row_end));
+    if (in.mode == IN_RING && lane == 31) sts_vol(in.cons, in.base + min(s0 + CB, row_end));
     if (lane == 0) recv = inv[0];
     tag_next = src_tag<KIND>(in, j + 1);
     src_load<KIND>(in, j + 1, ib[PAR ^ 1]);
-    int outq[C];
-    steps_chunk<KIND, R, PAR, CK, PD>(rec, cur, prv, recv, recv_prev, win, sym + s0 + C, bs, inv,
+    int outq[CB];
+    steps_chunk<KIND, R, PAR, CK, PD, CB>(rec, cur, prv, recv, recv_prev, win, sym + s0 + CB, bs, inv,
                                       outq, s0, lane, N, padmask, smax, sstep);
     const int pos = s0 - 32 * R;
     if (pos >= 0 && !dst_put(out, pos, outq, lane, W)) return false;
@@ -240,12 +249,12 @@ __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict_
   // Two chunk bodies per parity keep the code small (the instruction cache is
   // shared by every kind in flight on an SM): the steady one, and one that both
   // holds out-of-range cells and passes padding rows through (ramps, last band).
-  const int j_end = (N + 32 * R) / C;
+  const int j_end = (N + 32 * R) / CB;
   if (padwarp) {
     if (!range(0, j_end, T{}, T{})) return false;
   } else {
-    const int j_lo = min((32 * R) / C, j_end + 1);
-    const int j_hi = max(min((N - C + 1) / C, j_end), j_lo - 1);
+    const int j_lo = min((32 * R) / CB, j_end + 1);
+    const int j_hi = max(min((N - CB + 1) / CB, j_end), j_lo - 1);
     if (!range(0, j_lo - 1, T{}, T{})) return false;
     if (!range(j_lo, j_hi, F{}, F{})) return false;
     if (!range(j_hi + 1, j_end, T{}, T{})) return false;
@@ -285,7 +294,7 @@ __device__ void block_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob
   const int *a_sym = P.sym + jb.a_off;
   const int *b_sym = P.sym + jb.b_off;
   const int nb = (M + 32 * R - 1) / (32 * R);
-  const int L = ((N + 1 + C - 1) / C) * C + 2 * C;  // stream positions per band row
+  const int L = ((N + 1 + CB - 1) / CB) * CB + 2 * CB;  // stream positions per band row
   SwBest tb = {0, 0, 0, 0};
   int corner = 0, corner_band = -1;
   bool ok = true;
@@ -297,7 +306,7 @@ __device__ void block_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob
       in.mode = IN_TOP;
     } else if (warp == 0) {
       in.mode = IN_ROW; in.buf = S.u.wrap.row[(g - 1) & 1]; in.tags = S.u.wrap.tag[(g - 1) & 1];
-      in.base = (g - 1) * (L / C);
+      in.base = (g - 1) * (L / CB);
     } else {
       in.mode = IN_RING; in.buf = S.ring[warp]; in.tags = S.tag[warp]; in.cons = &S.cons[warp];
       in.base = g * L;
@@ -308,7 +317,7 @@ __device__ void block_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob
       out.mode = OUT_NONE;
     } else if (warp == NW - 1) {
       out.mode = OUT_ROW; out.buf = S.u.wrap.row[g & 1]; out.tags = S.u.wrap.tag[g & 1];
-      out.base = g * (L / C);
+      out.base = g * (L / CB);
     } else {
       out.mode = OUT_RING; out.buf = S.ring[warp + 1]; out.tags = S.tag[warp + 1];
       out.cons = &S.cons[warp + 1]; out.base = g * L;
@@ -390,9 +399,9 @@ __global__ void __launch_bounds__(NW * 32) batch_kernel(BatchParams P) {
   // phase 1: block jobs, one pair per CTA
   for (;;) {
     if (threadIdx.x == 0) S.job = S.abort ? P.n_b : atomicAdd(&P.ctrl[0], 1);
-    for (int i = threadIdx.x; i < NW * (RING / C); i += blockDim.x) (&S.tag[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < NW * (RING / CB); i += blockDim.x) (&S.tag[0][0])[i] = 0;
     for (int i = threadIdx.x; i < NW; i += blockDim.x) S.cons[i] = 0;
-    for (int i = threadIdx.x; i < 2 * (ROWSTRIDE_B / C); i += blockDim.x) (&S.u.wrap.tag[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < 2 * (ROWSTRIDE_B / CB); i += blockDim.x) (&S.u.wrap.tag[0][0])[i] = 0;
     __syncthreads();
     const int t = S.job;
     if (t >= P.n_b) break;

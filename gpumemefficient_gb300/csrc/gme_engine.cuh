@@ -87,20 +87,20 @@ __device__ __forceinline__ int4 ldg4(const int *p) { return __ldg(reinterpret_ca
 // hold their value.  PADROWS: rows beyond n2 copy the row above, so the warp's
 // bottom row equals row n2.
 // ---------------------------------------------------------------------------
-template <int KIND, int R, int PAR, bool CHECKED, bool PADROWS>
+template <int KIND, int R, int PAR, bool CHECKED, bool PADROWS, int CH = C>
 __device__ __forceinline__ void steps_chunk(const Rec<KIND> &rec, int (&cur)[R], int (&prv)[R],
-                                            int &recv, int &recv_prev, int (&win)[2 * C],
+                                            int &recv, int &recv_prev, int (&win)[2 * CH],
                                             const int *sym_next, const int (&bs)[R],
-                                            const int (&inv)[C], int (&outq)[C], int s0, int lane,
+                                            const int (&inv)[CH], int (&outq)[CH], int s0, int lane,
                                             int N, unsigned padmask, int (&smax)[R], int (&sstep)[R]) {
-  static_assert(R < C, "the window refill at step R needs R < C");
+  static_assert(R < CH, "the window refill at step R needs R < CH");
 #pragma unroll
-  for (int q = 0; q < C; ++q) {
+  for (int q = 0; q < CH; ++q) {
     if (q == R) {
 #pragma unroll
-      for (int i = 0; i < C / 4; ++i) {
+      for (int i = 0; i < CH / 4; ++i) {
         const int4 v = ldg4(sym_next + 4 * i);
-        const int h = (PAR ^ 1) * C + 4 * i;
+        const int h = (PAR ^ 1) * CH + 4 * i;
         win[h] = v.x; win[h + 1] = v.y; win[h + 2] = v.z; win[h + 3] = v.w;
       }
     }
@@ -111,7 +111,7 @@ __device__ __forceinline__ void steps_chunk(const Rec<KIND> &rec, int (&cur)[R],
 #pragma unroll
     for (int r = 0; r < R; ++r)
       D[r] = (r ? prv[r - 1] : recv_prev) +
-             (win[(PAR * C + q - r + 2 * C) % (2 * C)] == bs[r] ? rec.ceq : rec.cne);
+             (win[(PAR * CH + q - r + 2 * CH) % (2 * CH)] == bs[r] ? rec.ceq : rec.cne);
     int nv[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -133,7 +133,7 @@ __device__ __forceinline__ void steps_chunk(const Rec<KIND> &rec, int (&cur)[R],
         // lane 31 feeds the incoming row to lane 0 through the same shuffle; the
         // chunk's last step sends nothing useful: lane 0 re-latches the next
         // chunk's first column from the validated ring values
-        const int send = (lane == 31) ? inv[q + 1 < C ? q + 1 : C - 1] : v;
+        const int send = (lane == 31) ? inv[q + 1 < CH ? q + 1 : CH - 1] : v;
         recv = __shfl_sync(FULL, send, (lane + 31) & 31);  // for step s+1
         recv_prev = rcv;
       }
