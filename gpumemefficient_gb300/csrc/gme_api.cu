@@ -463,7 +463,7 @@ gme_status gme_align_batch(gme_context *ctx, const int32_t *symbols, int64_t nsy
       return to_status(results[i].status);
     }
   int bad = 0;
-  if ((e = cudaMemcpy(&bad, ctx->batch.d_ctrl + 2, sizeof(int), cudaMemcpyDeviceToHost)) == cudaSuccess && bad)
+  if ((e = cudaMemcpy(&bad, ctx->batch.d_ctrl + 8, sizeof(int), cudaMemcpyDeviceToHost)) == cudaSuccess && bad)
     return to_status(bad);
   return GME_OK;
 }

@@ -40,12 +40,13 @@ constexpr int ROWSTRIDE_G = BLOCK_MAXN + 32 * 8 + 3 * CB;  // a warp job's row i
 
 struct BatchParams {
   const int *sym;          // staged, padded symbols
-  const BatchJob *jobs_b;  // block jobs, longest first
-  const BatchJob *jobs_w;  // warp jobs, longest first
+  const BatchJob *jobs_b;  // block jobs, by kind, longest first
+  const BatchJob *jobs_w;  // warp jobs, by kind, longest first
   int n_b, n_w;
+  int kb[4], kw[4];        // jobs of kind k: jobs_b[kb[k]..kb[k+1]), jobs_w[kw[k]..kw[k+1])
   gme_result *results;
   int *rows;  // warp jobs: one row of ROWSTRIDE_G ints per warp of the grid (L2-resident)
-  int *ctrl;  // [0] block ticket, [1] warp ticket, [2] status
+  int *ctrl;  // [2k] block ticket of kind k, [2k+1] warp ticket of kind k, [8] status
   Scoring sc;
   unsigned long long timeout_ns;
 };
@@ -395,37 +396,44 @@ __global__ void __launch_bounds__(NW * 32) batch_kernel(BatchParams P) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) S.abort = 0;
   __syncthreads();
-  Waiter W(P.timeout_ns, &P.ctrl[2], &S.abort);
-  // phase 1: block jobs, one pair per CTA
-  for (;;) {
-    if (threadIdx.x == 0) S.job = S.abort ? P.n_b : atomicAdd(&P.ctrl[0], 1);
-    for (int i = threadIdx.x; i < NW * (RING / CB); i += blockDim.x) (&S.tag[0][0])[i] = 0;
-    for (int i = threadIdx.x; i < NW; i += blockDim.x) S.cons[i] = 0;
-    for (int i = threadIdx.x; i < 2 * (ROWSTRIDE_B / CB); i += blockDim.x) (&S.u.wrap.tag[0][0])[i] = 0;
-    __syncthreads();
-    const int t = S.job;
-    if (t >= P.n_b) break;
-    const BatchJob jb = P.jobs_b[t];
-    switch (jb.kind) {
-      case K_LCS: block_job<K_LCS, R, NW>(P, S, jb, warp, lane, W); break;
-      case K_ED: block_job<K_ED, R, NW>(P, S, jb, warp, lane, W); break;
-      default: block_job<K_SW, R, NW>(P, S, jb, warp, lane, W); break;
+  Waiter W(P.timeout_ns, &P.ctrl[8], &S.abort);
+  // One kind after another, so that an SM runs one kind's code at a time (the
+  // three kinds' loops do not fit the instruction cache together); within a kind
+  // first the large pairs one per CTA, then the rest one per warp.
+  for (int k = 0; k < 3; ++k) {
+    const int b0 = P.kb[k], nb = P.kb[k + 1] - b0, w0 = P.kw[k], nw = P.kw[k + 1] - w0;
+    // phase 1: block jobs, one pair per CTA
+    for (;;) {
+      if (threadIdx.x == 0) S.job = (S.abort || nb == 0) ? nb : atomicAdd(&P.ctrl[2 * k], 1);
+      for (int i = threadIdx.x; i < NW * (RING / CB); i += blockDim.x) (&S.tag[0][0])[i] = 0;
+      for (int i = threadIdx.x; i < NW; i += blockDim.x) S.cons[i] = 0;
+      for (int i = threadIdx.x; i < 2 * (ROWSTRIDE_B / CB); i += blockDim.x) (&S.u.wrap.tag[0][0])[i] = 0;
+      __syncthreads();
+      const int t = S.job;
+      if (t >= nb) break;
+      const BatchJob jb = P.jobs_b[b0 + t];
+      switch (k) {
+        case K_LCS: block_job<K_LCS, R, NW>(P, S, jb, warp, lane, W); break;
+        case K_ED: block_job<K_ED, R, NW>(P, S, jb, warp, lane, W); break;
+        default: block_job<K_SW, R, NW>(P, S, jb, warp, lane, W); break;
+      }
+      __syncthreads();
+    }
+    // phase 2: warp jobs, one pair per warp
+    for (;;) {
+      int t = 0;
+      if (lane == 0) t = (S.abort || nw == 0) ? nw : atomicAdd(&P.ctrl[2 * k + 1], 1);
+      t = __shfl_sync(FULL, t, 0);
+      if (t >= nw) break;
+      const BatchJob jb = P.jobs_w[w0 + t];
+      switch (k) {
+        case K_LCS: warp_job<K_LCS, R, NW>(P, S, jb, warp, lane, W); break;
+        case K_ED: warp_job<K_ED, R, NW>(P, S, jb, warp, lane, W); break;
+        default: warp_job<K_SW, R, NW>(P, S, jb, warp, lane, W); break;
+      }
+      if (*(volatile int *)&S.abort) break;
     }
     __syncthreads();
-  }
-  // phase 2: warp jobs, one small pair per warp
-  for (;;) {
-    int t = 0;
-    if (lane == 0) t = S.abort ? P.n_w : atomicAdd(&P.ctrl[1], 1);
-    t = __shfl_sync(FULL, t, 0);
-    if (t >= P.n_w) break;
-    const BatchJob jb = P.jobs_w[t];
-    switch (jb.kind) {
-      case K_LCS: warp_job<K_LCS, R, NW>(P, S, jb, warp, lane, W); break;
-      case K_ED: warp_job<K_ED, R, NW>(P, S, jb, warp, lane, W); break;
-      default: warp_job<K_SW, R, NW>(P, S, jb, warp, lane, W); break;
-    }
-    if (*(volatile int *)&S.abort) break;
   }
 }
 
@@ -555,6 +563,11 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
   ar.nseg = nseg;
   ar.n_b = (int)blockj.size();
   ar.n_w = (int)warpj.size();
+  // kind boundaries of the two queues (both are sorted by kind first)
+  for (int k = 0; k <= 3; ++k) {
+    ar.kb[k] = (int)(std::lower_bound(blockj.begin(), blockj.end(), k, [&](int i, int kk) { return pairs[i].kind < kk; }) - blockj.begin());
+    ar.kw[k] = (int)(std::lower_bound(warpj.begin(), warpj.end(), k, [&](int i, int kk) { return pairs[i].kind < kk; }) - warpj.begin());
+  }
   ar.NW = NW;
   int occ = batch_occupancy(NW);
   if (occ < 1) occ = 1;
@@ -573,7 +586,7 @@ int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring 
   *kernels = 0;
   if (ar.nseg == 0) return ST_OK;
   cudaError_t e;
-  if ((e = cudaMemsetAsync(ar.d_ctrl, 0, 4 * sizeof(int), st)) != cudaSuccess)
+  if ((e = cudaMemsetAsync(ar.d_ctrl, 0, 16 * sizeof(int), st)) != cudaSuccess)
     return ws.fail(e, "cudaMemsetAsync(batch ctrl)");
   const int blocks = (int)std::min<long long>(ar.nseg, 65535);
   batch_stage_kernel<<<blocks, 256, 0, st>>>(d_sym, ar.d_from, ar.d_to, ar.d_len, ar.d_padl,
@@ -585,6 +598,7 @@ int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring 
   P.jobs_w = ar.d_jobs + ar.n_b;
   P.n_b = ar.n_b;
   P.n_w = ar.n_w;
+  for (int k = 0; k < 4; ++k) { P.kb[k] = ar.kb[k]; P.kw[k] = ar.kw[k]; }
   P.results = d_results;
   P.rows = ar.d_rows;
   P.ctrl = ar.d_ctrl;

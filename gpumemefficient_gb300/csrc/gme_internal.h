@@ -69,6 +69,7 @@ struct BatchArena {
   // the plan
   long long nseg = 0;
   int n_b = 0, n_w = 0, NW = 4, grid = 0;
+  int kb[4] = {0, 0, 0, 0}, kw[4] = {0, 0, 0, 0};  // per-kind offsets into the two queues
   std::vector<int> longj;             // result slots of pairs for the plain path
   std::vector<gme_pair> long_pairs;   // their descriptors
   bool sync_before_reuse = true;      // wait for the stream before overwriting the plan
