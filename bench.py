@@ -39,6 +39,7 @@ import numpy as np  # noqa: E402
 OPS_PER_CELL = {0: 4, 1: 7, 2: 8}
 KIND_NAME = {0: "LCS", 1: "ED", 2: "SW"}
 INT_LANES_PER_SM = 128
+METRIC = "GCUPS on 1 GB300, batched/served vs plain per-pair (bit-exact); p50/p99 latency"
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -155,7 +156,7 @@ def run_reference(args):
     cells = len(a) * rows
     tot = sum(times)
     val = cells * len(times) / tot / 1e9
-    line = {"impl": "reference", "metric": "GCUPS on 1 GB300 (bit-exact)", "value": val, "unit": "GCUPS",
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GCUPS",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * tot / len(times), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded)", "config": cfg,
@@ -185,7 +186,7 @@ def run_reference_batch(args, ws):
     val = cells * len(times) / tot / 1e9
     cfg = {"workload": f"batched: {len(kinds)} pairs, lengths log-uniform [64, 4096], alphabet 4, "
                        "LCS/ED/SW 1/3 each", "pairs": len(kinds), "seed": synth.SEED_BATCH}
-    line = {"impl": "reference", "metric": "GCUPS on 1 GB300 (bit-exact)", "value": val, "unit": "GCUPS",
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GCUPS",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded)", "config": cfg,
@@ -299,7 +300,7 @@ def run_gme(args):
     cfg = dict(cfg)
     cfg.update({"l2": "flushed between timed steps (256 MiB write)", "plain_config": ctx.plain_config(n1, n2),
                 "parity_vs_oracle": "ok" if parity else "MISMATCH", "score": int(res.score)})
-    line = {"metric": "GCUPS on 1 GB300 (bit-exact)", "value": value, "unit": "GCUPS", "n_gpus": ws,
+    line = {"metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * mean_s,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded)", "config": cfg, "clocks": clk, "e2e": e2e,
@@ -448,7 +449,7 @@ def run_gme_batch(args):
            "l2": "flushed between timed steps (256 MiB write)", "parity_vs_oracle": "ok" if parity else "MISMATCH",
            "plain_per_pair_gcups": plain_gcups, "plain_sample_pairs": int(len(sub)),
            "batched_over_plain": value / ws / plain_gcups}
-    line = {"metric": "GCUPS on 1 GB300 (bit-exact)", "value": value, "unit": "GCUPS", "n_gpus": ws,
+    line = {"metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * mean_s,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded)", "config": cfg, "clocks": clk, "e2e": e2e,
@@ -460,6 +461,178 @@ def run_gme_batch(args):
     ctx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def _percentiles(lat_ns):
+    if len(lat_ns) == 0:
+        return {"p50_ms": None, "p99_ms": None}
+    return {"p50_ms": float(np.percentile(lat_ns, 50)) / 1e6, "p99_ms": float(np.percentile(lat_ns, 99)) / 1e6,
+            "max_ms": float(np.max(lat_ns)) / 1e6}
+
+
+def _collect_served(srv, want):
+    """Drains the server and takes `want` results: (tickets, results, latencies) in completion order."""
+    if not srv.drain(600):
+        raise RuntimeError("served: drain timed out")
+    ts, rs, ls = [], [], []
+    got = 0
+    while got < want:
+        t, r, l = srv.poll_many(65536)
+        if len(t) == 0:
+            break
+        ts.append(t); rs.append(r); ls.append(l)
+        got += len(t)
+    return np.concatenate(ts), np.concatenate(rs), np.concatenate(ls)
+
+
+def run_gme_served(args):
+    """Served path: the request stream submitted open loop; saturation GCUPS, then a
+    Poisson arrival-rate sweep with p50/p99 latency; the same requests as one batch."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    import __graft_entry__ as ge
+    ge.build()
+    import gpumemefficient_gb300 as g
+    from gpumemefficient_gb300 import synth
+    from oracle import oracle as O
+
+    symbols, pairs = synth.served_requests(args.requests)
+    n = len(pairs)
+    kinds = pairs["kind"]
+    cells_k = pairs["n1"].astype(np.float64) * pairs["n2"]
+    cells = float(cells_k.sum())
+    ops = float(sum(cells_k[kinds == k].sum() * OPS_PER_CELL[k] for k in range(3)))
+    sc = g.scoring()
+    srv = g.Server(local, sc=sc, waves=args.waves)
+
+    # parity of every request with the oracle (outside the timed region)
+    tick = srv.submit_many(symbols, pairs)
+    t_, r_, _ = _collect_served(srv, n)
+    order = np.argsort(t_)
+    res = r_[order]
+    assert (np.sort(t_) == np.sort(tick)).all()
+    sa = [symbols[o:o + k] for o, k in zip(pairs["a_off"], pairs["n1"])]
+    sb = [symbols[o:o + k] for o, k in zip(pairs["b_off"], pairs["n2"])]
+    o = O.align_batch(kinds, sa, sb, threads=os.cpu_count() or 1)
+    sw = kinds == 2
+    parity = bool((res["status"] == 0).all() and (res["score"] == o["score"]).all() and
+                  (res["sw_max"][sw] == o["sw_max"][sw]).all() and (res["sw_max_y"][sw] == o["sw_y"][sw]).all()
+                  and (res["sw_max_x"][sw] == o["sw_x"][sw]).all())
+
+    for _ in range(args.warmup):
+        srv.submit_many(symbols, pairs)
+        _collect_served(srv, n)
+    # saturation: every request of the stream arrives at once, each step waits for all
+    st0 = srv.stats()
+    clocks = ClockSampler(local)
+    time.sleep(0.15)
+    times, lat_sat = [], None
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        srv.submit_many(symbols, pairs)
+        _, _, lat_sat = _collect_served(srv, n)
+        times.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    st1 = srv.stats()
+    t_tot = sum(times)
+    value = cells * len(times) / t_tot / 1e9
+
+    # arrival-rate sweep: Poisson arrivals at a fraction of the saturation throughput
+    rng = np.random.default_rng(synth.SEED_SERVE + 1)
+    mean_cells = cells / n
+    sweep = []
+    for frac in args.rates:
+        lam = frac * value * 1e9 / mean_cells          # requests per second
+        m = int(min(n, max(200, lam * args.rate_seconds)))
+        idx = rng.permutation(n)[:m]
+        arr = np.cumsum(rng.exponential(1.0 / lam, m))
+        sub_pairs = pairs[idx]
+        call_t = np.zeros(m)
+        t0 = time.perf_counter()
+        i = 0
+        while i < m:
+            now = time.perf_counter() - t0
+            j = int(np.searchsorted(arr, now, side="right"))
+            if j > i:
+                srv.submit_many(symbols, sub_pairs[i:j])
+                call_t[i:j] = time.perf_counter() - t0
+                i = j
+            else:
+                wait = arr[i] - now
+                if wait > 2e-4:
+                    time.sleep(wait - 1e-4)
+        tk, rr, ll = _collect_served(srv, m)
+        t_end = time.perf_counter() - t0
+        # open-loop latency: from the scheduled arrival, so a late submission counts
+        first = int(tk.min())
+        late = (call_t - arr)[(tk - first).astype(np.int64)]
+        lat = ll + late * 1e9
+        sweep.append({"offered_fraction": frac, "requests": m, "offered_gcups": frac * value,
+                      "achieved_gcups": float(cells_k[idx].sum()) / t_end / 1e9,
+                      **_percentiles(lat), "max_submit_lag_ms": float(late.max() * 1e3),
+                      "ok": bool((rr["status"] == 0).all())})
+
+    # the same requests as one planned batch (graph replay, inputs resident)
+    ctx = g.Context(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=local)
+    sp = stream.cuda_stream
+    with torch.cuda.stream(stream):
+        d_sym = torch.from_numpy(symbols).to(dev)
+        d_res = torch.zeros(n * g.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    stream.synchronize()
+    plan = g.BatchPlan(ctx, pairs, len(symbols))
+    for _ in range(3):
+        plan.run(d_sym.data_ptr(), d_res.data_ptr(), stream=sp, use_graph=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        plan.run(d_sym.data_ptr(), d_res.data_ptr(), stream=sp, use_graph=True)
+    e1.record(stream)
+    stream.synchronize()
+    batched = cells * args.steps / (e0.elapsed_time(e1) / 1e3) / 1e9
+    plan.close()
+    ctx.close()
+
+    props = torch.cuda.get_device_properties(local)
+    sms = props.multi_processor_count
+    mhz = clk.get("sm_mhz") or 1920.0
+    peak_tops = sms * INT_LANES_PER_SM * mhz * 1e6 / 1e12
+    achieved = ops * len(times) / t_tot / 1e12
+    roof = {"bound": "int_alu", "achieved": achieved, "peak": peak_tops, "unit": "Tops/s",
+            "frac": achieved / peak_tops, "traffic": None,
+            "peak_basis": f"{sms} SMs x {INT_LANES_PER_SM} INT32 lanes x median SM clock {mhz:.0f} MHz under load",
+            "ops_per_cell": "ED 7, SW 8 weighted by cells", "kernel": "batch_kernel (served, host clock)"}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        k = min(n, 400)
+        t0 = time.perf_counter()
+        O.align_batch(kinds[:k], sa[:k], sb[:k], threads=os.cpu_count() or 1)
+        dt = time.perf_counter() - t0
+        cpu = {"value": float(cells_k[:k].sum()) / dt / 1e9, "unit": "GCUPS", "cores": os.cpu_count(),
+               "kind": "port", "sample": f"first {k} of the {n} requests ({cells_k[:k].sum():.3g} cells), "
+                                         f"oracle/oracle.c pairs across {os.cpu_count()} threads, {dt:.2f} s"}
+    h2d = int(symbols.nbytes + n * (pairs.itemsize + 64))
+    d2h = int(n * (g.RESULT_DTYPE.itemsize + 4))
+    cfg = {"workload": f"served: {n} requests per step, half ED half SW, lengths log-uniform [32, 16384], "
+                       "alphabet 4, submitted open loop to the server (host queue, HBM-budget admission, "
+                       "launch slots on separate streams, completion flags in pinned memory)",
+           "requests": n, "cells": cells, "seed": synth.SEED_SERVE, "hbm_budget_bytes": st1["hbm_budget_bytes"],
+           "hbm_bytes_peak": st1["hbm_bytes_peak"], "waves_per_step": (st1["waves_launched"] - st0["waves_launched"]) / len(times),
+           "l2": "inputs (172 MB of symbols per step) larger than L2", "parity_vs_oracle": "ok" if parity else "MISMATCH",
+           "saturation_latency": _percentiles(lat_sat), "rate_sweep": sweep,
+           "batched_same_requests_gcups": batched, "served_over_batched": value / batched}
+    line = {"metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_tot / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded)", "config": cfg, "clocks": clk,
+            "e2e": {"value": value, "unit": "GCUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "note": "the served path is end to end: host symbols in, host results out"},
+            "gpu_launches": int(st1["kernels_launched"] - st0["kernels_launched"]), "roofline": roof,
+            "cpu_baseline": cpu}
+    srv.close()
+    return line
 
 
 def main():
@@ -474,6 +647,11 @@ def main():
     p.add_argument("--plain-sample", type=int, default=256,
                    help="batched workload: pairs timed one by one on the plain path")
     p.add_argument("--batch-warps", type=int, default=0, help="batched workload: warps per CTA")
+    p.add_argument("--requests", type=int, default=8192, help="served workload: requests per step")
+    p.add_argument("--waves", type=int, default=0, help="served workload: launch slots (0 = default)")
+    p.add_argument("--rates", type=float, nargs="*", default=[0.1, 0.5, 0.8],
+                   help="served workload: offered load as fractions of the saturation throughput")
+    p.add_argument("--rate-seconds", type=float, default=2.0, help="served workload: seconds per rate point")
     args = p.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -481,6 +659,8 @@ def main():
         run_reference(args)
     elif args.workload == "batched":
         run_gme_batch(args)
+    elif args.workload == "served":
+        print(json.dumps(run_gme_served(args)), flush=True)
     else:
         run_gme(args)
 

@@ -56,13 +56,27 @@ class Pair(ctypes.Structure):
 
 class BatchConfig(ctypes.Structure):
     _fields_ = [("warps_per_block", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
-                ("block_min_cells", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("block_min_cells", ctypes.c_int64), ("long_min_cells", ctypes.c_int64),
+                ("team_min_cells", ctypes.c_int64)]
 
 
 PAIR_DTYPE = np.dtype([("a_off", "<i8"), ("b_off", "<i8"), ("n1", "<i4"), ("n2", "<i4"),
                        ("kind", "<i4"), ("reserved", "<i4")])
 RESULT_DTYPE = np.dtype([("score", "<i4"), ("sw_max", "<i4"), ("sw_max_y", "<i8"),
                          ("sw_max_x", "<i8"), ("status", "<i4"), ("kind", "<i4")])
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("wave_max_cells", ctypes.c_int64),
+                ("waves", ctypes.c_int32), ("queue_max", ctypes.c_int32),
+                ("warps_per_block", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in (
+        "submitted", "completed", "queued", "running", "waves_launched", "kernels_launched",
+        "cells_completed", "hbm_bytes_held", "hbm_bytes_peak", "hbm_budget_bytes", "h2d_bytes",
+        "d2h_bytes")]
 
 
 class PlainConfig(ctypes.Structure):
@@ -96,10 +110,21 @@ def _declare(L):
     L.gme_align_batch_device.argtypes = [_vp, _vp, c.c_int64, _vp, c.c_int64, c.POINTER(Scoring),
                                          _vp, _vp]
     L.gme_batch_stats.argtypes = [_vp, c.POINTER(c.c_int64), c.POINTER(c.c_int64),
-                                  c.POINTER(c.c_int64)]
+                                  c.POINTER(c.c_int64), c.POINTER(c.c_int64)]
     L.gme_batch_plan_create.argtypes = [_vp, _vp, c.c_int64, c.c_int64, c.POINTER(c.c_void_p)]
     L.gme_batch_plan_run.argtypes = [_vp, _vp, c.POINTER(Scoring), _vp, _vp, c.c_int]
     L.gme_batch_plan_destroy.argtypes = [_vp]
+    L.gme_server_create.argtypes = [c.c_int, c.POINTER(ServerConfig), c.POINTER(Scoring),
+                                    c.POINTER(c.c_void_p)]
+    L.gme_server_destroy.argtypes = [_vp]
+    L.gme_submit.argtypes = [_vp, c.c_int, _vp, c.c_int64, _vp, c.c_int64, c.POINTER(c.c_uint64)]
+    L.gme_submit_many.argtypes = [_vp, _vp, _vp, c.c_int64, _vp, c.POINTER(c.c_int64)]
+    L.gme_poll.argtypes = [_vp, c.c_uint64, c.POINTER(Result), c.POINTER(c.c_int64)]
+    L.gme_poll_many.argtypes = [_vp, _vp, _vp, _vp, c.c_int64, c.POINTER(c.c_int64)]
+    L.gme_server_drain.argtypes = [_vp, c.c_uint64]
+    L.gme_server_get_stats.argtypes = [_vp, c.POINTER(ServerStats)]
+    L.gme_server_last_error.argtypes = [_vp]
+    L.gme_server_last_error.restype = c.c_char_p
     L.gme_debug_wait_timeout.argtypes = [_vp, c.c_uint64, c.POINTER(c.c_int32)]
     L.gme_launch_count.argtypes = [_vp]
     L.gme_launch_count.restype = c.c_int64
@@ -213,14 +238,15 @@ class Context:
                                       stream or None), self.handle)
 
     def set_batch_config(self, warps_per_block: int = 0, blocks_per_sm: int = 0,
-                         block_min_cells: int = 0):
-        cfg = BatchConfig(warps_per_block, blocks_per_sm, block_min_cells, 0)
+                         block_min_cells: int = 0, long_min_cells: int = 0, team_min_cells: int = 0):
+        cfg = BatchConfig(warps_per_block, blocks_per_sm, block_min_cells, long_min_cells, team_min_cells)
         _check(lib().gme_set_batch_config(self.handle, ctypes.byref(cfg)), self.handle)
 
     def batch_stats(self) -> dict:
-        b, w, l = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
-        _check(lib().gme_batch_stats(self.handle, ctypes.byref(b), ctypes.byref(w), ctypes.byref(l)))
-        return {"block_jobs": b.value, "warp_jobs": w.value, "long_jobs": l.value}
+        b, w, l, t = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().gme_batch_stats(self.handle, ctypes.byref(b), ctypes.byref(w), ctypes.byref(l),
+                                     ctypes.byref(t)))
+        return {"block_jobs": b.value, "warp_jobs": w.value, "long_jobs": l.value, "team_jobs": t.value}
 
     def align_batch(self, kinds, seqs_a, seqs_b, sc: Optional[Scoring] = None) -> np.ndarray:
         """Many alignments in one launch; returns a structured array of results."""
@@ -275,6 +301,102 @@ class BatchPlan:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """The served path: submit alignments one at a time, collect each as it finishes.
+
+    A native dispatcher thread admits queued requests against the HBM budget and
+    launches them in waves on several streams; results and completion flags come
+    back through pinned host memory (``include/gme.h``, served path).
+    """
+
+    NOT_READY = 7
+
+    def __init__(self, device: int = 0, sc: Optional[Scoring] = None, hbm_budget_bytes: int = 0,
+                 wave_max_cells: int = 0, waves: int = 0, queue_max: int = 0,
+                 warps_per_block: int = 0):
+        cfg = ServerConfig(hbm_budget_bytes, wave_max_cells, waves, queue_max, warps_per_block, 0)
+        self.sc = sc or scoring()
+        h = ctypes.c_void_p()
+        _check(lib().gme_server_create(device, ctypes.byref(cfg), ctypes.byref(self.sc),
+                                       ctypes.byref(h)))
+        self.handle = h
+
+    def _err(self, st):
+        if st != 0:
+            raise GmeError(st, lib().gme_server_last_error(self.handle).decode())
+
+    def submit(self, kind, a, b) -> int:
+        """Queues one alignment; returns its ticket (a and b are copied)."""
+        kind = KINDS.get(kind, kind) if isinstance(kind, str) else kind
+        a = np.ascontiguousarray(a, dtype=np.int32)
+        b = np.ascontiguousarray(b, dtype=np.int32)
+        t = ctypes.c_uint64()
+        self._err(lib().gme_submit(self.handle, int(kind), a.ctypes.data, len(a), b.ctypes.data,
+                                   len(b), ctypes.byref(t)))
+        return t.value
+
+    def submit_many(self, symbols: np.ndarray, pairs: np.ndarray) -> np.ndarray:
+        """Queues len(pairs) alignments (PAIR_DTYPE over one int32 symbol buffer); returns tickets."""
+        symbols = np.ascontiguousarray(symbols, np.int32)
+        pairs = np.ascontiguousarray(pairs, PAIR_DTYPE)
+        tickets = np.zeros(len(pairs), np.uint64)
+        k = ctypes.c_int64()
+        self._err(lib().gme_submit_many(self.handle, symbols.ctypes.data, pairs.ctypes.data, len(pairs),
+                                        tickets.ctypes.data, ctypes.byref(k)))
+        return tickets
+
+    def poll(self, ticket: int):
+        """(result dict, latency_ns) once done, else None."""
+        r = Result()
+        lat = ctypes.c_int64()
+        st = lib().gme_poll(self.handle, ticket, ctypes.byref(r), ctypes.byref(lat))
+        if st == self.NOT_READY:
+            return None
+        self._err(st)
+        return ({"score": r.score, "sw_max": r.sw_max, "sw_max_y": r.sw_max_y,
+                 "sw_max_x": r.sw_max_x, "status": r.status, "kind": r.kind}, lat.value)
+
+    def poll_many(self, max_n: int = 65536):
+        """(tickets, RESULT_DTYPE results, latencies in ns) of requests finished since the last call."""
+        tickets = np.zeros(max_n, np.uint64)
+        res = np.zeros(max_n, RESULT_DTYPE)
+        lat = np.zeros(max_n, np.int64)
+        n = ctypes.c_int64()
+        self._err(lib().gme_poll_many(self.handle, tickets.ctypes.data, res.ctypes.data,
+                                      lat.ctypes.data, max_n, ctypes.byref(n)))
+        k = n.value
+        return tickets[:k], res[:k], lat[:k]
+
+    def drain(self, timeout_s: float = 600.0) -> bool:
+        st = lib().gme_server_drain(self.handle, int(timeout_s * 1e9))
+        if st == self.NOT_READY:
+            return False
+        self._err(st)
+        return True
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        self._err(lib().gme_server_get_stats(self.handle, ctypes.byref(s)))
+        return {n: getattr(s, n) for n, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().gme_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def pack_batch(kinds, seqs_a, seqs_b):

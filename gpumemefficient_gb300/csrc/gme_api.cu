@@ -36,7 +36,9 @@ static int grow(void **p, long long *cap, long long need, size_t elem, Workspace
     return ws.fail(e, what);
   }
   if (zero) {
+    // the library's streams do not wait for the null stream: finish the clear here
     e = cudaMemset(*p, 0, (size_t)n * elem);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
     if (e != cudaSuccess) return ws.fail(e, what);
   }
   *cap = n;
@@ -58,7 +60,9 @@ int Workspace::reserve(long long a_len, long long b_len, long long slot_words, i
   if (!ctrl) {
     cudaError_t e = cudaMalloc(&ctrl, 16 * sizeof(int));
     if (e != cudaSuccess) return fail(e, "cudaMalloc(ctrl)");
-    cudaMemset(ctrl, 0, 16 * sizeof(int));
+    e = cudaMemset(ctrl, 0, 16 * sizeof(int));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+    if (e != cudaSuccess) return fail(e, "cudaMemset(ctrl)");
   }
   return ST_OK;
 }
@@ -99,10 +103,33 @@ int BatchArena::reserve_rows(long long ints, Workspace &ws) {
   return grow_ll((void **)&d_rows, &rows_cap, ints, sizeof(int), ws, "cudaMalloc(batch rows)");
 }
 
+// Wrap-row tags come from one counter that only grows, so a row never holds a tag
+// that a later job is handed, whatever the layout of the rows (fresh rows are zero).
+int BatchArena::reserve_wrap(long long words, Workspace &ws) {
+  int rc;
+  if ((rc = grow((void **)&d_wrap, &wrap_cap, words, 8, ws, "cudaMalloc(batch wrap rows)", true))) return rc;
+  if (!d_gen) {
+    long long gc = 0;
+    if ((rc = grow((void **)&d_gen, &gc, 1, 4, ws, "cudaMalloc(batch wrap tags)", true))) return rc;
+  }
+  return ST_OK;
+}
+
+int BatchArena::reserve_team(long long units, long long bytes, Workspace &ws) {
+  int rc;
+  if ((rc = grow_ll((void **)&d_units, &units_cap, std::max(units, 1ll), sizeof(int4), ws, "cudaMalloc(batch team units)")))
+    return rc;
+  return grow_ll((void **)&d_team, &team_cap, std::max(bytes, 16ll), 1, ws, "cudaMalloc(batch teams)");
+}
+
 void BatchArena::release() {
   cudaFree(d_rows);
   d_rows = nullptr;
   rows_cap = 0;
+  cudaFree(d_wrap); cudaFree(d_gen);
+  d_wrap = nullptr; d_gen = nullptr; wrap_cap = 0;
+  cudaFree(d_units); cudaFree(d_team);
+  d_units = nullptr; d_team = nullptr; units_cap = team_cap = 0;
   cudaFree(d_staged); cudaFree(d_from); cudaFree(d_to); cudaFree(d_len); cudaFree(d_padl);
   cudaFree(d_total); cudaFree(d_jobs); cudaFree(d_ctrl);
   d_staged = nullptr; d_from = d_to = nullptr; d_len = d_padl = d_total = nullptr; d_jobs = nullptr;
@@ -406,9 +433,13 @@ gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg) {
       }
       t.warps_per_block = cfg->warps_per_block;
     }
-    if (cfg->blocks_per_sm < 0 || cfg->block_min_cells < 0) return GME_ERR_INVALID;
+    if (cfg->blocks_per_sm < 0 || cfg->block_min_cells < 0 || cfg->long_min_cells < -1 ||
+        cfg->team_min_cells < -1)
+      return GME_ERR_INVALID;
     t.blocks_per_sm = cfg->blocks_per_sm;
     if (cfg->block_min_cells) t.block_min_cells = cfg->block_min_cells;
+    t.long_min_cells = cfg->long_min_cells;
+    if (cfg->team_min_cells) t.team_min_cells = cfg->team_min_cells;
   }
   ctx->batch_tune = t;
   return GME_OK;
@@ -502,6 +533,11 @@ gme_status gme_batch_plan_create(gme_context *ctx, const gme_pair *pairs, int64_
   p->npairs = npairs;
   p->max_len_sum = mx;
   int rc = gme::batch_plan(ctx->ws, p->ar, pairs, npairs, nsym, ctx->batch_tune, ctx->stream);
+  // runs may come on other streams: the descriptors must have landed first
+  if (rc == ST_OK) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) rc = ctx->ws.fail(e, "cudaStreamSynchronize(batch plan)");
+  }
   if (rc != ST_OK) {
     p->ar.release();
     delete p;
@@ -510,6 +546,7 @@ gme_status gme_batch_plan_create(gme_context *ctx, const gme_pair *pairs, int64_
   ctx->batch.last_block_jobs = p->ar.last_block_jobs;
   ctx->batch.last_warp_jobs = p->ar.last_warp_jobs;
   ctx->batch.last_long_jobs = p->ar.last_long_jobs;
+  ctx->batch.last_team_jobs = p->ar.last_team_jobs;
   *out = p;
   return GME_OK;
 }
@@ -579,11 +616,12 @@ gme_status gme_batch_plan_destroy(gme_batch_plan *p) {
 }
 
 gme_status gme_batch_stats(const gme_context *ctx, int64_t *block_jobs, int64_t *warp_jobs,
-                           int64_t *long_jobs) {
+                           int64_t *long_jobs, int64_t *team_jobs) {
   if (!ctx) return GME_ERR_INVALID;
   if (block_jobs) *block_jobs = ctx->batch.last_block_jobs;
   if (warp_jobs) *warp_jobs = ctx->batch.last_warp_jobs;
   if (long_jobs) *long_jobs = ctx->batch.last_long_jobs;
+  if (team_jobs) *team_jobs = ctx->batch.last_team_jobs;
   return GME_OK;
 }
 
@@ -597,3 +635,34 @@ gme_status gme_debug_wait_timeout(gme_context *ctx, uint64_t timeout_ns, int32_t
 int64_t gme_launch_count(const gme_context *ctx) { return ctx ? ctx->ws.launches : -1; }
 
 }  // extern "C"
+
+namespace gme {
+
+cudaStream_t ctx_stream(gme_context *ctx) { return ctx->stream; }
+
+void ctx_set_served(gme_context *ctx, int *d_done) {
+  ctx->batch.d_done = d_done;
+  ctx->batch.sync_before_reuse = d_done == nullptr;
+}
+
+long long ctx_device_bytes(const gme_context *ctx) {
+  const Workspace &w = ctx->ws;
+  const BatchArena &b = ctx->batch;
+  long long n = 4 * (w.a_pad_cap + w.b_pad_cap) + 8 * w.slots_cap + 32ll * w.best_cap + (w.ctrl ? 64 : 0);
+  n += 4 * (b.staged_cap + b.rows_cap) + 28 * b.seg_cap + (long long)sizeof(BatchJob) * b.jobs_cap +
+       8 * b.wrap_cap + (b.d_gen ? 4 * 1025 : 0) + (b.d_ctrl ? 64 : 0) + 16 * b.units_cap + b.team_cap;
+  n += 4 * (ctx->d_a_cap + ctx->d_b_cap + ctx->d_row_cap + ctx->d_col_cap + ctx->d_bsym_cap) +
+       (long long)sizeof(gme_result) * (ctx->d_bres_cap + 1);
+  return n;
+}
+
+int ctx_sms(const gme_context *ctx) { return ctx->ws.sms; }
+
+int ctx_batch_status(gme_context *ctx) {
+  int v = 0;
+  if (!ctx->batch.d_ctrl) return 0;
+  if (cudaMemcpy(&v, ctx->batch.d_ctrl + 8, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return ST_CUDA;
+  return v;
+}
+
+}  // namespace gme

@@ -14,6 +14,7 @@
 // Replaces, for many pairs at once, the reference's one-pair-per-call host
 // functions (EditDistance/GPU_Hyperlane_Share.cu:689-789 and its LCS/SW twins).
 #include <algorithm>
+#include <climits>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -32,21 +33,38 @@ namespace gme {
 constexpr int CB = GME_BATCH_CHUNK;
 
 
-constexpr int BLOCK_MAXN = 4096;  // widest pair (n1) the batch kernel takes (rows in shared or L2)
+constexpr int BATCH_MAXN = BATCH_MAX_N1;
 // a row is read up to one chunk past the last chunk (the read-ahead): j_end+1 with
-// j_end = (n1 + 32R)/CB, so a row of n1 columns needs n1 + 32R + 2C entries (R <= 8)
-constexpr int ROWSTRIDE_B = BLOCK_MAXN + 32 * 8 + 3 * CB;
-constexpr int ROWSTRIDE_G = BLOCK_MAXN + 32 * 8 + 3 * CB;  // a warp job's row in global memory
+// j_end = (n1 + 32R)/CB, so a row of n1 columns needs n1 + 32R + 2C entries (R <= 8);
+// rows are laid out with the stride of the batch's widest pair
+__host__ __device__ constexpr int row_stride(int max_n1) { return (max_n1 + 32 * 8 + 3 * CB + 7) / 8 * 8; }
+
+// A pair shared by a team of T CTAs: member t sweeps band groups t, t+T, t+2T, ...
+// handing each group's bottom row to the next member through the job's two tagged
+// rows.  The members combine their results here; the last one to finish writes it.
+struct __align__(16) TeamSlot {
+  unsigned long long best;  // SW: (value << 32) | ~(y*(n1+1)+x), so the maximum is the first best cell
+  int corner;               // stored value of the last band's bottom row at column n1
+  int done;                 // members finished
+};
 
 struct BatchParams {
   const int *sym;          // staged, padded symbols
   const BatchJob *jobs_b;  // block jobs, by kind, longest first
   const BatchJob *jobs_w;  // warp jobs, by kind, longest first
+  const BatchJob *jobs_t;  // team jobs, by kind, longest first
+  const int4 *units;       // team members {team job, member t, team size T, 0}, by kind
   int n_b, n_w;
-  int kb[4], kw[4];        // jobs of kind k: jobs_b[kb[k]..kb[k+1]), jobs_w[kw[k]..kw[k+1])
+  int kb[4], kw[4], ku[4]; // kind k: jobs_b[kb[k]..kb[k+1]), jobs_w[kw[k]..), units[ku[k]..)
+  TeamSlot *team;          // one per team job (cleared by every launch)
+  unsigned long long *twrap;  // two tagged rows of `stride` words per team job (cleared likewise)
   gme_result *results;
-  int *rows;  // warp jobs: one row of ROWSTRIDE_G ints per warp of the grid (L2-resident)
-  int *ctrl;  // [2k] block ticket of kind k, [2k+1] warp ticket of kind k, [8] status
+  int *done;               // optional: done[index] = 1 once results[index] is written (system scope)
+  int *rows;               // warp jobs: one row of `stride` ints per warp of the grid (L2-resident)
+  unsigned long long *wrap;  // block jobs: two tagged rows of `stride` words per CTA
+  unsigned *gen;           // tags handed out to wrap rows so far (kept across launches)
+  int stride;
+  int *ctrl;               // [2k] block ticket of kind k, [2k+1] warp ticket, [8] status, [10+k] team ticket
   Scoring sc;
   unsigned long long timeout_ns;
 };
@@ -55,14 +73,10 @@ template <int NW> struct __align__(16) BatchSmem {
   int ring[NW][RING];       // ring[w]: warp w-1 -> warp w (w >= 1)
   int tag[NW][RING / CB];
   int cons[NW];
-  union {
-    struct {
-      int row[2][ROWSTRIDE_B];  // warp NW-1 -> warp 0 across band groups
-      int tag[2][ROWSTRIDE_B / CB];
-    } wrap;
-  } u;
   int job;
+  int phase;
   int abort;
+  unsigned gen;
   SwBest best[NW];
 };
 
@@ -76,60 +90,91 @@ enum : int { OUT_NONE = 0, OUT_RING = 1, OUT_ROW = 2, OUT_OWN = 3 };
 
 struct Src {
   int mode;
-  const int *buf;   // ring or row values
-  const int *tags;  // ring or row chunk tags
-  int *cons;        // ring: consumption counter (stream position)
-  int base;         // ring: stream position of column 0; row: tag generation
-  int rule;         // top border: ED boundary rule
+  const int *buf;                  // ring values, or the warp's own row
+  const int *tags;                 // ring chunk tags
+  const unsigned long long *row;   // IN_ROW: tagged words {tag, value} in global memory
+  int *cons;                       // ring: consumption counter (stream position)
+  int base;                        // ring: stream position of column 0
+  unsigned tag;                    // IN_ROW: the tag of the row wanted
+  int rule;                        // top border: ED boundary rule
 };
 
 struct Dst {
   int mode;
   int *buf;
   int *tags;
+  unsigned long long *row;
   const int *cons;
   int base;
+  unsigned tag;
   int cons_seen;
 };
 
-template <int KIND>
-__device__ __forceinline__ int src_tag(const Src &s, int j) {
-  if (s.mode == IN_RING) return ld_acquire_cta(&s.tags[(s.base / CB + j) & (RING / CB - 1)]);
-  if (s.mode == IN_ROW) return ld_acquire_cta(&s.tags[j]);
-  return 0;
+__device__ __forceinline__ void ld_vol_u64x2(const unsigned long long *p, unsigned long long &a,
+                                             unsigned long long &b) {
+  asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2];" : "=l"(a), "=l"(b) : "l"(p));
 }
-__device__ __forceinline__ int src_want(const Src &s, int j) {
-  if (s.mode == IN_RING) return s.base / CB + j + 1;
-  if (s.mode == IN_ROW) return s.base + j + 1;
-  return 0;
+__device__ __forceinline__ void st_vol_u64x2(unsigned long long *p, unsigned long long a,
+                                             unsigned long long b) {
+  asm volatile("st.volatile.global.v2.u64 [%0], {%1,%2};" :: "l"(p), "l"(a), "l"(b) : "memory");
 }
+
+// Chunk j of the incoming row into d[]; returns whether it is ready (the same in
+// every lane: all lanes read the same words).  A ring chunk's tag is acquired
+// before its values; a global row's tag travels in the same 64-bit word as the
+// value, so the row needs no fence on either side.
 template <int KIND>
-__device__ __forceinline__ void src_load(const Src &s, int j, int (&d)[CB]) {
+__device__ __forceinline__ bool src_fetch(const Src &s, int j, int (&d)[CB]) {
   if (s.mode == IN_TOP) {
 #pragma unroll
     for (int k = 0; k < CB; ++k) d[k] = Rec<KIND>::top(CB * j + k, s.rule);
-    return;
+    return true;
   }
-  const int *p = (s.mode == IN_RING) ? s.buf + ((s.base + CB * j) & (RING - 1)) : s.buf + CB * j;
+  if (s.mode == IN_ROW) {
+    const unsigned long long *p = s.row + CB * j;
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < CB; k += 2) {
+      unsigned long long w0, w1;
+      ld_vol_u64x2(p + k, w0, w1);
+      d[k] = (int)(unsigned)w0;
+      d[k + 1] = (int)(unsigned)w1;
+      ok &= (unsigned)(w0 >> 32) == s.tag && (unsigned)(w1 >> 32) == s.tag;
+    }
+    return ok;
+  }
   if (s.mode == IN_OWN) {
     // the warp's own row in global memory, written by lane 31 one band earlier:
     // read at L2 (.cg) so that no lane sees a line its L1 kept from before the write
+    const int *p = s.buf + CB * j;
 #pragma unroll
     for (int k = 0; k < CB; k += 4) {
       const int4 q = __ldcg(reinterpret_cast<const int4 *>(p + k));
       d[k] = q.x; d[k + 1] = q.y; d[k + 2] = q.z; d[k + 3] = q.w;
     }
-    return;
+    return true;
   }
+  const bool ok = ld_acquire_cta(&s.tags[(s.base / CB + j) & (RING / CB - 1)]) == s.base / CB + j + 1;
+  const int *p = s.buf + ((s.base + CB * j) & (RING - 1));
 #pragma unroll
   for (int k = 0; k < CB; k += 4) {
     const int4 q = *reinterpret_cast<const int4 *>(p + k);
     d[k] = q.x; d[k + 1] = q.y; d[k + 2] = q.z; d[k + 3] = q.w;
   }
+  return ok;
 }
 
 __device__ __forceinline__ bool dst_put(Dst &o, int pos, const int (&q)[CB], int lane, Waiter &W) {
   if (o.mode == OUT_NONE) return true;
+  if (o.mode == OUT_ROW) {
+    if (lane == 31) {
+      const unsigned long long t = (unsigned long long)o.tag << 32;
+#pragma unroll
+      for (int k = 0; k < CB; k += 2)
+        st_vol_u64x2(o.row + pos + k, t | (unsigned)q[k], t | (unsigned)q[k + 1]);
+    }
+    return true;
+  }
   int *p;
   if (o.mode == OUT_RING) {
     const int sp = o.base + pos;
@@ -149,7 +194,6 @@ __device__ __forceinline__ bool dst_put(Dst &o, int pos, const int (&q)[CB], int
     for (int k = 0; k < CB; k += 4)
       *reinterpret_cast<int4 *>(p + k) = make_int4(q[k], q[k + 1], q[k + 2], q[k + 3]);
     if (o.mode == OUT_RING) st_release_cta(&o.tags[((o.base + pos) / CB) & (RING / CB - 1)], (o.base + pos) / CB + 1);
-    else if (o.mode == OUT_ROW) st_release_cta(&o.tags[pos / CB], o.base + pos / CB + 1);
   }
   return true;
 }
@@ -202,8 +246,7 @@ __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict_
   const int row_end = ((N + 1 + CB - 1) / CB) * CB;  // ring positions carrying this row
   int recv = 0, recv_prev = 0;
   int ib[2][CB];
-  int tag_next = src_tag<KIND>(in, 0);
-  src_load<KIND>(in, 0, ib[0]);
+  bool ok_next = src_fetch<KIND>(in, 0, ib[0]);
 
   auto chunk = [&](int j, auto par, auto checked, auto padrows) -> bool {
     constexpr int PAR = decltype(par)::value;
@@ -211,17 +254,14 @@ __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict_
     int(&inv)[CB] = ib[PAR];
     const int s0 = CB * j;
     __syncwarp();
-    if (s0 <= N && !__all_sync(FULL, tag_next == src_want(in, j))) {
-      auto ready = [&] { return __all_sync(FULL, src_tag<KIND>(in, j) == src_want(in, j)); };
-      if (!W.wait(ready)) return false;
-      src_load<KIND>(in, j, inv);
+    if (s0 <= N && !__all_sync(FULL, ok_next)) {
+      if (!W.wait([&] { return __all_sync(FULL, src_fetch<KIND>(in, j, inv)); })) return false;
     }
     // consumed: this chunk, but never past the end of this band's row -- the ring's
     // next positions already belong to the next band group of the same pair
     if (in.mode == IN_RING && lane == 31) sts_vol(in.cons, in.base + min(s0 + CB, row_end));
     if (lane == 0) recv = inv[0];
-    tag_next = src_tag<KIND>(in, j + 1);
-    src_load<KIND>(in, j + 1, ib[PAR ^ 1]);
+    ok_next = src_fetch<KIND>(in, j + 1, ib[PAR ^ 1]);
     int outq[CB];
     steps_chunk<KIND, R, PAR, CK, PD, CB>(rec, cur, prv, recv, recv_prev, win, sym + s0 + CB, bs, inv,
                                       outq, s0, lane, N, padmask, smax, sstep);
@@ -285,12 +325,33 @@ __device__ __forceinline__ SwBest warp_best(SwBest b) {
   return b;
 }
 
-// A whole pair on one CTA: warp w sweeps bands w, w+NW, w+2NW, ...; band b takes
-// its incoming row from warp b-1 (ring[w]) or, for w = 0, from the wrap row the
-// last warp wrote in the previous group.
+// A job's status: a timeout if any wait of this CTA or of the launch gave up (a
+// team member's result may then be incomplete).
+__device__ __forceinline__ int job_status(const BatchParams &P, const int &abort) {
+  return (*(const volatile int *)&abort || ld_relaxed_gpu_s32(&P.ctrl[8])) ? ST_TIMEOUT : 0;
+}
+
+// A job's result, then (if asked for) its completion flag, ordered at system
+// scope so that a host thread polling the flag in mapped memory sees the result.
+__device__ __forceinline__ void put_result(const BatchParams &P, int index, const gme_result &r) {
+  P.results[index] = r;
+  if (P.done) {
+    __threadfence_system();
+    *(volatile int *)&P.done[index] = 1;
+  }
+}
+
+// A pair on a CTA, or on member t of a team of T CTAs: warp w sweeps bands
+// g*NW + w of the groups g = t, t+T, t+2T, ...; band b takes its incoming row from
+// warp b-1 (ring[w]) or, for w = 0, from the wrap row that warp NW-1 wrote for
+// group g-1 (on this CTA, or on the previous member).  The wrap rows are two
+// tagged rows in global memory, alternating by group; group g's row carries tag
+// tag0 + g + 1.  A CTA's own rows (T = 1) take tag0 from a counter that only grows,
+// so no row holds a tag handed out later; a team's rows are cleared at launch.
 template <int KIND, int R, int NW>
 __device__ void block_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob &jb, int warp,
-                          int lane, Waiter &W) {
+                          int lane, Waiter &W, int t, int T, unsigned long long *wrap, unsigned tag0,
+                          TeamSlot *team) {
   const int N = jb.n1, M = jb.n2;
   const int *a_sym = P.sym + jb.a_off;
   const int *b_sym = P.sym + jb.b_off;
@@ -299,29 +360,29 @@ __device__ void block_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob
   SwBest tb = {0, 0, 0, 0};
   int corner = 0, corner_band = -1;
   bool ok = true;
-  for (int g = 0; ok && g * NW + warp < nb; ++g) {
+  // ring stream positions count this CTA's groups (i), so that every ring starts
+  // at position 0 with its consumption counter; the wrap rows go by the group (g)
+  for (int g = t, i = 0; ok && g * NW + warp < nb; g += T, ++i) {
     const int band = g * NW + warp;
     Src in;
     in.rule = P.sc.ed_rule;
     if (band == 0) {
       in.mode = IN_TOP;
     } else if (warp == 0) {
-      in.mode = IN_ROW; in.buf = S.u.wrap.row[(g - 1) & 1]; in.tags = S.u.wrap.tag[(g - 1) & 1];
-      in.base = (g - 1) * (L / CB);
+      in.mode = IN_ROW; in.row = wrap + ((g - 1) & 1) * P.stride; in.tag = tag0 + g;
     } else {
       in.mode = IN_RING; in.buf = S.ring[warp]; in.tags = S.tag[warp]; in.cons = &S.cons[warp];
-      in.base = g * L;
+      in.base = i * L;
     }
     Dst out;
     out.cons_seen = 0;
     if (band == nb - 1) {
       out.mode = OUT_NONE;
     } else if (warp == NW - 1) {
-      out.mode = OUT_ROW; out.buf = S.u.wrap.row[g & 1]; out.tags = S.u.wrap.tag[g & 1];
-      out.base = g * (L / CB);
+      out.mode = OUT_ROW; out.row = wrap + (g & 1) * P.stride; out.tag = tag0 + g + 1;
     } else {
       out.mode = OUT_RING; out.buf = S.ring[warp + 1]; out.tags = S.tag[warp + 1];
-      out.cons = &S.cons[warp + 1]; out.base = g * L;
+      out.cons = &S.cons[warp + 1]; out.base = i * L;
     }
     int c = 0;
     ok = sweep_band<KIND, R>(P.sc, a_sym, b_sym, N, M, band * 32 * R, lane, in, out, W, c, tb);
@@ -333,19 +394,47 @@ __device__ void block_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob
     if (lane == 0) S.best[warp] = tb;
   }
   __syncthreads();
+  SwBest b = {0, 0, 0, 0};
+  if (KIND == K_SW)
+    for (int k = 0; k < NW; ++k)
+      if (better(S.best[k], b)) b = S.best[k];
+  if (T == 1) {
+    if (corner_band >= 0 && lane == 31) {
+      gme_result r;
+      r.score = Rec<KIND>::to_v(corner, N, M);
+      r.sw_max = b.v;
+      r.sw_max_y = b.y;
+      r.sw_max_x = b.x;
+      r.status = job_status(P, S.abort);
+      r.kind = KIND;
+      put_result(P, jb.index, r);
+    }
+    return;
+  }
+  // a team: publish this member's part, the last member to finish writes the result
   if (corner_band >= 0 && lane == 31) {
-    gme_result r;
-    r.score = Rec<KIND>::to_v(corner, N, M);
-    SwBest b = {0, 0, 0, 0};
-    if (KIND == K_SW)
-      for (int k = 0; k < NW; ++k)
-        if (better(S.best[k], b)) b = S.best[k];
-    r.sw_max = b.v;
-    r.sw_max_y = b.y;
-    r.sw_max_x = b.x;
-    r.status = 0;
-    r.kind = KIND;
-    P.results[jb.index] = r;
+    *(volatile int *)&team->corner = corner;
+    __threadfence();
+  }
+  if (KIND == K_SW && threadIdx.x == 0 && b.v > 0)
+    atomicMax(&team->best, ((unsigned long long)(unsigned)b.v << 32) |
+                               (0xffffffffu - (unsigned)(b.y * (N + 1) + b.x)));
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&team->done, 1) == T - 1) {
+      __threadfence();
+      gme_result r;
+      r.score = Rec<KIND>::to_v(*(volatile int *)&team->corner, N, M);
+      const unsigned long long k = KIND == K_SW ? atomicAdd(&team->best, 0ull) : 0ull;
+      r.sw_max = (int)(k >> 32);
+      const long long lin = r.sw_max ? (long long)(0xffffffffu - (unsigned)k) : 0;
+      r.sw_max_y = r.sw_max ? lin / (N + 1) : 0;
+      r.sw_max_x = r.sw_max ? lin % (N + 1) : 0;
+      r.status = job_status(P, S.abort);
+      r.kind = KIND;
+      put_result(P, jb.index, r);
+    }
   }
 }
 
@@ -357,7 +446,7 @@ __device__ void warp_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob 
   const int *a_sym = P.sym + jb.a_off;
   const int *b_sym = P.sym + jb.b_off;
   const int nb = (M + 32 * R - 1) / (32 * R);
-  int *row = P.rows + ((long long)blockIdx.x * NW + warp) * ROWSTRIDE_G;
+  int *row = P.rows + ((long long)blockIdx.x * NW + warp) * P.stride;
   SwBest tb = {0, 0, 0, 0};
   int corner = 0;
   for (int band = 0; band < nb; ++band) {
@@ -383,9 +472,9 @@ __device__ void warp_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob 
     r.sw_max = KIND == K_SW ? b0.v : 0;
     r.sw_max_y = KIND == K_SW ? b0.y : 0;
     r.sw_max_x = KIND == K_SW ? b0.x : 0;
-    r.status = 0;
+    r.status = job_status(P, S.abort);
     r.kind = KIND;
-    P.results[jb.index] = r;
+    put_result(P, jb.index, r);
   }
 }
 
@@ -402,20 +491,56 @@ __global__ void __launch_bounds__(NW * 32) batch_kernel(BatchParams P) {
   // first the large pairs one per CTA, then the rest one per warp.
   for (int k = 0; k < 3; ++k) {
     const int b0 = P.kb[k], nb = P.kb[k + 1] - b0, w0 = P.kw[k], nw = P.kw[k + 1] - w0;
-    // phase 1: block jobs, one pair per CTA
+    const int u0 = P.ku[k], nu = P.ku[k + 1] - u0;
+    // phase 1: members of team jobs (claimed in order, so a member waits only on
+    // members claimed before it, all of them running), then block jobs, one pair
+    // per CTA; one call site per kind keeps the loop's code small
+    if (threadIdx.x == 0) S.phase = 0;
     for (;;) {
-      if (threadIdx.x == 0) S.job = (S.abort || nb == 0) ? nb : atomicAdd(&P.ctrl[2 * k], 1);
+      if (threadIdx.x == 0) {
+        int job = -1;
+        if (!S.abort && S.phase == 0) {
+          const int t = nu ? atomicAdd(&P.ctrl[10 + k], 1) : nu;
+          if (t < nu) job = t;
+          else S.phase = 1;
+        }
+        if (!S.abort && S.phase == 1) {
+          const int t = nb ? atomicAdd(&P.ctrl[2 * k], 1) : nb;
+          if (t < nb) {
+            job = t;
+            // tags for the job's wrap rows, one per band group, never used before
+            const int n2 = P.jobs_b[b0 + t].n2;
+            S.gen = atomicAdd(P.gen, (unsigned)((n2 + 32 * R * NW - 1) / (32 * R * NW)));
+          }
+        }
+        S.job = job;
+      }
       for (int i = threadIdx.x; i < NW * (RING / CB); i += blockDim.x) (&S.tag[0][0])[i] = 0;
       for (int i = threadIdx.x; i < NW; i += blockDim.x) S.cons[i] = 0;
-      for (int i = threadIdx.x; i < 2 * (ROWSTRIDE_B / CB); i += blockDim.x) (&S.u.wrap.tag[0][0])[i] = 0;
       __syncthreads();
       const int t = S.job;
-      if (t >= nb) break;
-      const BatchJob jb = P.jobs_b[b0 + t];
+      if (t < 0) break;
+      BatchJob jb;
+      int mt = 0, mT = 1;
+      unsigned long long *wrap;
+      unsigned tag0 = 0;
+      TeamSlot *team = nullptr;
+      if (S.phase == 0) {
+        const int4 u = P.units[u0 + t];
+        jb = P.jobs_t[u.x];
+        mt = u.y;
+        mT = u.z;
+        wrap = P.twrap + (long long)u.x * 2 * P.stride;
+        team = &P.team[u.x];
+      } else {
+        jb = P.jobs_b[b0 + t];
+        wrap = P.wrap + (long long)blockIdx.x * 2 * P.stride;
+        tag0 = S.gen;
+      }
       switch (k) {
-        case K_LCS: block_job<K_LCS, R, NW>(P, S, jb, warp, lane, W); break;
-        case K_ED: block_job<K_ED, R, NW>(P, S, jb, warp, lane, W); break;
-        default: block_job<K_SW, R, NW>(P, S, jb, warp, lane, W); break;
+        case K_LCS: block_job<K_LCS, R, NW>(P, S, jb, warp, lane, W, mt, mT, wrap, tag0, team); break;
+        case K_ED: block_job<K_ED, R, NW>(P, S, jb, warp, lane, W, mt, mT, wrap, tag0, team); break;
+        default: block_job<K_SW, R, NW>(P, S, jb, warp, lane, W, mt, mT, wrap, tag0, team); break;
       }
       __syncthreads();
     }
@@ -489,6 +614,25 @@ int batch_occupancy(int NW) {
 
 bool batch_config_valid(int NW) { return NW == 4 || NW == 8; }
 
+// Device bytes one pair adds to a batch: its symbols as the caller holds them, the
+// staged copy (pads, b rounded up to whole band groups) and its descriptors.
+long long batch_pair_bytes(long long n1, long long n2) {
+  const long long staged = (PADL + n1 + PADR + 3) / 4 * 4 + (n2 + 32 * 4 * 8 - 1) / (32 * 4 * 8) * (32 * 4 * 8);
+  return 4 * (n1 + n2) + 4 * staged + 2 * 32 + (long long)sizeof(BatchJob);
+}
+
+// CTAs of the batch kernel's grid.
+long long batch_grid(int sms, int NW, int blocks_per_sm) {
+  int occ = batch_occupancy(NW);
+  if (occ < 1) occ = 1;
+  return (long long)sms * std::min(occ, blocks_per_sm > 0 ? blocks_per_sm : occ);
+}
+
+// Device bytes of a batch's per-CTA rows (warp jobs' rows, block jobs' wrap rows).
+long long batch_scratch_bytes(long long grid, int NW, int max_n1) {
+  return grid * row_stride(max_n1) * (4ll * NW + 2 * 8);
+}
+
 // The plan: classify the pairs (per warp, per CTA, or plain path), order them
 // longest first, lay the staged symbols out and upload the descriptors.  Waits
 // for the arena's previous work on `st` before reusing its buffers.
@@ -497,15 +641,34 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
   constexpr int R = 4;
   const int NW = tune.warps_per_block;
   if (!batch_config_valid(NW)) return ws.fail_msg(ST_INVALID, "batch: warps_per_block must be 4 or 8");
-  std::vector<int> blockj, warpj;
+  std::vector<int> blockj, warpj, teamj;
   ar.longj.clear();
+  int occ0 = batch_occupancy(NW);
+  if (occ0 < 1) occ0 = 1;
+  const int grid0 = ws.sms * std::min(occ0, tune.blocks_per_sm > 0 ? tune.blocks_per_sm : occ0);
+  long long total_cells = 0;
   for (long long i = 0; i < npairs; ++i) {
     const gme_pair &p = pairs[i];
     if (p.n1 < 0 || p.n2 < 0 || p.kind < 0 || p.kind > 2 || p.a_off < 0 || p.b_off < 0 ||
         p.a_off + p.n1 > nsym || p.b_off + p.n2 > nsym)
       return ws.fail_msg(ST_INVALID, "batch: pair " + std::to_string(i) + " out of range");
-    if (p.n1 == 0 || p.n2 == 0 || p.n1 > BLOCK_MAXN) ar.longj.push_back((int)i);
-    else if ((long long)p.n1 * p.n2 >= tune.block_min_cells && p.n2 > 32 * R * (NW - 1)) blockj.push_back((int)i);
+    total_cells += (long long)p.n1 * p.n2;
+  }
+  // the plain path takes a pair only when even a team of 8 CTAs would outlast an
+  // even share of the batch (and always pairs too wide for the rows, or empty)
+  long long long_min = tune.long_min_cells;
+  if (long_min == 0) long_min = std::max(1ll << 27, 8 * (total_cells / grid0));
+  if (long_min < 0) long_min = LLONG_MAX;
+  const long long team_min = tune.team_min_cells > 0 ? tune.team_min_cells : LLONG_MAX;
+  auto groups = [&](const gme_pair &p) { return ((p.n2 + 32 * R - 1) / (32 * R) + NW - 1) / NW; };
+  for (long long i = 0; i < npairs; ++i) {
+    const gme_pair &p = pairs[i];
+    const long long cells = (long long)p.n1 * p.n2;
+    if (p.n1 == 0 || p.n2 == 0 || p.n1 > BATCH_MAXN || cells >= long_min)
+      ar.longj.push_back((int)i);
+    else if (cells >= team_min && groups(p) >= 4 && (long long)(p.n1 + 1) * (p.n2 + 1) < (1ll << 32))
+      teamj.push_back((int)i);
+    else if (cells >= tune.block_min_cells && p.n2 > 32 * R * (NW - 1)) blockj.push_back((int)i);
     else warpj.push_back((int)i);
   }
   // one kind after another (an SM then runs one kind's code at a time), longest first
@@ -516,12 +679,13 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
   };
   std::sort(blockj.begin(), blockj.end(), by_cells);
   std::sort(warpj.begin(), warpj.end(), by_cells);
+  std::sort(teamj.begin(), teamj.end(), by_cells);
   ar.long_pairs.clear();
   for (int i : ar.longj) ar.long_pairs.push_back(pairs[i]);
   // staged layout: a padded with PADL/PADR at a 16-byte aligned start, b padded to whole bands
-  const long long nseg = 2 * (long long)(blockj.size() + warpj.size());
+  const long long nseg = 2 * (long long)(blockj.size() + warpj.size() + teamj.size());
   ar.h_from.resize(nseg); ar.h_to.resize(nseg); ar.h_len.resize(nseg); ar.h_padl.resize(nseg); ar.h_total.resize(nseg);
-  ar.h_jobs.resize(blockj.size() + warpj.size());
+  ar.h_jobs.resize(blockj.size() + warpj.size() + teamj.size());
   long long off = 0, seg = 0;
   auto place = [&](long long from, int len, int padl, int total) {
     ar.h_from[seg] = from; ar.h_to[seg] = off; ar.h_len[seg] = len; ar.h_padl[seg] = padl; ar.h_total[seg] = total;
@@ -542,39 +706,57 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
   size_t slot = 0;
   for (int i : blockj) add(i, 32 * R * NW, slot++);
   for (int i : warpj) add(i, 32 * R, slot++);
+  // a team of T = groups/2 (2..8) CTAs per team job; members claimed in order
+  ar.h_units.clear();
+  for (size_t j = 0; j < teamj.size(); ++j) {
+    add(teamj[j], 32 * R * NW, slot++);
+    const int G = (int)groups(pairs[teamj[j]]);
+    const int T = std::max(2, std::min(8, G / 2));
+    for (int t = 0; t < T; ++t) ar.h_units.push_back(make_int4((int)j, t, T, 0));
+  }
   cudaError_t e;
   if (ar.sync_before_reuse && (e = cudaStreamSynchronize(st)) != cudaSuccess)
     return ws.fail(e, "cudaStreamSynchronize(batch arena)");
   int rc = ar.reserve(off + 64, nseg, (long long)ar.h_jobs.size(), ws);
   if (rc != ST_OK) return rc;
-  int occ0 = batch_occupancy(NW);
-  if (occ0 < 1) occ0 = 1;
-  const int grid0 = ws.sms * std::min(occ0, tune.blocks_per_sm > 0 ? tune.blocks_per_sm : occ0);
-  if ((rc = ar.reserve_rows((long long)grid0 * NW * ROWSTRIDE_G, ws)) != ST_OK) return rc;
+  int max_n1 = 0;
+  for (const BatchJob &j : ar.h_jobs) max_n1 = std::max(max_n1, j.n1);
+  ar.stride = row_stride(max_n1);
+  ar.n_t = (int)teamj.size();
+  ar.team_bytes = (long long)ar.n_t * (sizeof(TeamSlot) + 2ll * ar.stride * 8);
+  if ((rc = ar.reserve_rows((long long)grid0 * NW * ar.stride, ws)) != ST_OK) return rc;
+  if ((rc = ar.reserve_wrap((long long)grid0 * 2 * ar.stride, ws)) != ST_OK) return rc;
+  if ((rc = ar.reserve_team((long long)ar.h_units.size(), ar.team_bytes, ws)) != ST_OK) return rc;
+  if (!ar.h_units.empty() &&
+      (e = cudaMemcpyAsync(ar.d_units, ar.h_units.data(), ar.h_units.size() * sizeof(int4), cudaMemcpyHostToDevice, st)))
+    return ws.fail(e, "cudaMemcpyAsync(batch team units)");
   if (nseg > 0) {
-    if ((e = cudaMemcpy(ar.d_from, ar.h_from.data(), nseg * 8, cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(ar.d_to, ar.h_to.data(), nseg * 8, cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(ar.d_len, ar.h_len.data(), nseg * 4, cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(ar.d_padl, ar.h_padl.data(), nseg * 4, cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(ar.d_total, ar.h_total.data(), nseg * 4, cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(ar.d_jobs, ar.h_jobs.data(), ar.h_jobs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice)))
-      return ws.fail(e, "cudaMemcpy(batch plan)");
+    // pageable sources: each call has copied its bytes out before it returns, and
+    // the copies are ordered before the launches that read them on `st`
+    if ((e = cudaMemcpyAsync(ar.d_from, ar.h_from.data(), nseg * 8, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(ar.d_to, ar.h_to.data(), nseg * 8, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(ar.d_len, ar.h_len.data(), nseg * 4, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(ar.d_padl, ar.h_padl.data(), nseg * 4, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(ar.d_total, ar.h_total.data(), nseg * 4, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(ar.d_jobs, ar.h_jobs.data(), ar.h_jobs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice, st)))
+      return ws.fail(e, "cudaMemcpyAsync(batch plan)");
   }
   ar.nseg = nseg;
   ar.n_b = (int)blockj.size();
   ar.n_w = (int)warpj.size();
-  // kind boundaries of the two queues (both are sorted by kind first)
+  // kind boundaries of the queues (all sorted by kind first)
   for (int k = 0; k <= 3; ++k) {
     ar.kb[k] = (int)(std::lower_bound(blockj.begin(), blockj.end(), k, [&](int i, int kk) { return pairs[i].kind < kk; }) - blockj.begin());
     ar.kw[k] = (int)(std::lower_bound(warpj.begin(), warpj.end(), k, [&](int i, int kk) { return pairs[i].kind < kk; }) - warpj.begin());
+    ar.ku[k] = (int)(std::lower_bound(ar.h_units.begin(), ar.h_units.end(), k, [&](const int4 &u, int kk) {
+                       return pairs[teamj[u.x]].kind < kk; }) - ar.h_units.begin());
   }
   ar.NW = NW;
-  int occ = batch_occupancy(NW);
-  if (occ < 1) occ = 1;
-  ar.grid = ws.sms * std::min(occ, tune.blocks_per_sm > 0 ? tune.blocks_per_sm : occ);
+  ar.grid = grid0;
   ar.last_block_jobs = ar.n_b;
   ar.last_warp_jobs = ar.n_w;
   ar.last_long_jobs = (long long)ar.longj.size();
+  ar.last_team_jobs = ar.n_t;
   return ST_OK;
 }
 
@@ -588,6 +770,8 @@ int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring 
   cudaError_t e;
   if ((e = cudaMemsetAsync(ar.d_ctrl, 0, 16 * sizeof(int), st)) != cudaSuccess)
     return ws.fail(e, "cudaMemsetAsync(batch ctrl)");
+  if (ar.team_bytes > 0 && (e = cudaMemsetAsync(ar.d_team, 0, (size_t)ar.team_bytes, st)) != cudaSuccess)
+    return ws.fail(e, "cudaMemsetAsync(batch teams)");
   const int blocks = (int)std::min<long long>(ar.nseg, 65535);
   batch_stage_kernel<<<blocks, 256, 0, st>>>(d_sym, ar.d_from, ar.d_to, ar.d_len, ar.d_padl,
                                              ar.d_total, (int)ar.nseg, ar.d_staged);
@@ -596,11 +780,19 @@ int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring 
   P.sym = ar.d_staged;
   P.jobs_b = ar.d_jobs;
   P.jobs_w = ar.d_jobs + ar.n_b;
+  P.jobs_t = ar.d_jobs + ar.n_b + ar.n_w;
+  P.units = ar.d_units;
   P.n_b = ar.n_b;
   P.n_w = ar.n_w;
-  for (int k = 0; k < 4; ++k) { P.kb[k] = ar.kb[k]; P.kw[k] = ar.kw[k]; }
+  for (int k = 0; k < 4; ++k) { P.kb[k] = ar.kb[k]; P.kw[k] = ar.kw[k]; P.ku[k] = ar.ku[k]; }
+  P.team = reinterpret_cast<TeamSlot *>(ar.d_team);
+  P.twrap = reinterpret_cast<unsigned long long *>(ar.d_team + (long long)ar.n_t * sizeof(TeamSlot));
   P.results = d_results;
+  P.done = ar.d_done;
   P.rows = ar.d_rows;
+  P.wrap = ar.d_wrap;
+  P.gen = ar.d_gen;
+  P.stride = ar.stride;
   P.ctrl = ar.d_ctrl;
   P.sc = sc;
   P.timeout_ns = timeout_ns;

@@ -51,7 +51,12 @@ struct BatchTuning {
   int warps_per_block = 4;  // compute warps of a CTA (block jobs pipeline them over bands)
   int blocks_per_sm = 0;    // 0 = as many as fit
   long long block_min_cells = 1ll << 22;  // pairs at least this large (and with a band per warp) run one per CTA
-
+  // pairs at least this large run on the plain path (many CTAs each); 0 = automatic:
+  // max(2^27, 8 x the batch's cells / CTAs), i.e. only a pair that even a team of 8
+  // CTAs would take longer on than an even share of the batch; < 0 = never
+  long long long_min_cells = 0;
+  // pairs at least this large (with 4+ band groups) run on a team of CTAs; < 0 = never
+  long long team_min_cells = 1ll << 25;
 };
 
 // Device and host buffers of the batched path, owned by a context, grown on demand.
@@ -65,6 +70,17 @@ struct BatchArena {
   BatchJob *d_jobs = nullptr; long long jobs_cap = 0;
   int *d_ctrl = nullptr;
   int *d_rows = nullptr; long long rows_cap = 0;  // warp jobs' rows
+  unsigned long long *d_wrap = nullptr; long long wrap_cap = 0;  // block jobs' tagged wrap rows
+  unsigned *d_gen = nullptr;                                     // the tags they have used
+  int stride = 0;                                                // row stride of the plan
+  int *d_done = nullptr;  // completion flags (served path), or null
+  std::vector<int4> h_units;                          // team members {job, t, T, 0}
+  int4 *d_units = nullptr; long long units_cap = 0;
+  char *d_team = nullptr; long long team_cap = 0;      // team slots, then their wrap rows
+  long long team_bytes = 0;                           // the part of it the plan uses
+  int n_t = 0;
+  int ku[4] = {0, 0, 0, 0};
+  long long last_team_jobs = 0;
   long long last_block_jobs = 0, last_warp_jobs = 0, last_long_jobs = 0;
   // the plan
   long long nseg = 0;
@@ -75,12 +91,18 @@ struct BatchArena {
   bool sync_before_reuse = true;      // wait for the stream before overwriting the plan
   int reserve(long long staged, long long nseg, long long njobs, Workspace &ws);
   int reserve_rows(long long ints, Workspace &ws);
+  int reserve_wrap(long long words, Workspace &ws);
+  int reserve_team(long long units, long long bytes, Workspace &ws);
   void release();
 };
 
 // batched path (gme_batch.cu)
 bool batch_config_valid(int NW);
 int batch_occupancy(int NW);
+constexpr int BATCH_MAX_N1 = 16384;  // widest pair the batch kernel takes (wider: plain path)
+long long batch_pair_bytes(long long n1, long long n2);
+long long batch_grid(int sms, int NW, int blocks_per_sm);
+long long batch_scratch_bytes(long long grid, int NW, int max_n1);
 int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long npairs,
                long long nsym, const BatchTuning &tune, cudaStream_t st);
 int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring &sc,
@@ -102,5 +124,15 @@ int plain_run(Workspace &ws, int kind, const int *d_a, long long n1, const int *
               cudaStream_t st, int R, int NW, int grid, unsigned long long timeout_ns);
 int debug_wait_timeout(Workspace &ws, unsigned long long timeout_ns, int *kernel_status,
                        cudaStream_t st);
+
+// internals of a context the served path drives (gme_api.cu)
+cudaStream_t ctx_stream(gme_context *ctx);
+// completion flags for the context's batches (null: none); its batches then trust
+// the caller to reuse the arena only after the previous batch has finished
+void ctx_set_served(gme_context *ctx, int *d_done);
+long long ctx_device_bytes(const gme_context *ctx);
+int ctx_sms(const gme_context *ctx);
+// the status word of the context's last batch kernel (read after it has finished)
+int ctx_batch_status(gme_context *ctx);
 
 }  // namespace gme

@@ -82,3 +82,26 @@ def batch_pairs(npairs: int = 16384, lo: int = 64, hi: int = 4096, alphabet: int
     seqs_a = [uniform(int(n), alphabet, rng) for n in la]
     seqs_b = [uniform(int(n), alphabet, rng) for n in lb]
     return kinds, seqs_a, seqs_b
+
+
+def served_requests(n: int = 8192, lo: int = 32, hi: int = 16384, alphabet: int = 4,
+                    seed: int = SEED_SERVE):
+    """Request stream of the served workload: half edit distance, half Smith-Waterman,
+    each length log-uniform in [lo, hi], symbols uniform.  Returns (symbols, pairs)
+    with pairs a PAIR_DTYPE array over the one symbol buffer (request order = arrival order)."""
+    from . import PAIR_DTYPE
+    rng = np.random.default_rng(seed)
+    la = np.exp(rng.uniform(np.log(lo), np.log(hi), n)).astype(np.int64)
+    lb = np.exp(rng.uniform(np.log(lo), np.log(hi), n)).astype(np.int64)
+    kinds = np.repeat(np.array([1, 2], np.int32), (n + 1) // 2)[:n]
+    rng.shuffle(kinds)
+    lens = np.stack([la, lb], 1).reshape(-1)
+    offs = np.concatenate([[0], np.cumsum(lens)[:-1]])
+    symbols = rng.integers(0, alphabet, int(lens.sum()), dtype=np.int64).astype(np.int32)
+    pairs = np.zeros(n, PAIR_DTYPE)
+    pairs["a_off"] = offs[0::2]
+    pairs["b_off"] = offs[1::2]
+    pairs["n1"] = la
+    pairs["n2"] = lb
+    pairs["kind"] = kinds
+    return symbols, pairs

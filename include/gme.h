@@ -117,12 +117,14 @@ gme_status gme_align_device(gme_context *ctx, gme_kind kind, const int32_t *d_a,
 /* ---- batched path: many alignments in one launch --------------------------------
  * Pair i reads a = symbols[a_off .. a_off+n1), b = symbols[b_off .. b_off+n2) and
  * computes `kind` with the shared scoring; result i gets its score (and SW maximum).
- * One persistent work-queue kernel runs every pair whose n1 <= 4096: pairs of at
- * least block_min_cells cells (and at least one band of 128 rows per warp) one per
- * CTA (the CTA's warps pipelined over the pair's bands), all others one per warp;
- * kinds one after another, longest first.  Wider or empty
- * pairs run on the plain path, one launch each, on the same stream.  Replaces calling
- * the reference's one-pair host function (e.g. EditDistance/GPU_Hyperlane_Share.cu:689)
+ * One persistent work-queue kernel runs every pair whose n1 <= 16384, kinds one
+ * after another and within a kind longest first: pairs of at least team_min_cells
+ * cells on a team of 2..8 CTAs (each CTA takes every T-th group of row bands),
+ * pairs of at least block_min_cells cells (and at least one band of 128 rows per
+ * warp) one per CTA (the CTA's warps pipelined over the pair's bands), all others
+ * one per warp.  Wider, empty or very large (see long_min_cells) pairs run on the
+ * plain path, one launch each, on the same stream.  Replaces calling the
+ * reference's one-pair host function (e.g. EditDistance/GPU_Hyperlane_Share.cu:689)
  * once per pair. */
 typedef struct gme_pair {
   int64_t a_off, b_off; /* element offsets into the symbol buffer */
@@ -134,8 +136,13 @@ typedef struct gme_pair {
 typedef struct gme_batch_config {
   int32_t warps_per_block; /* 4 or 8 (0 = automatic) */
   int32_t blocks_per_sm;   /* CTAs per SM (0 = as many as fit) */
-  int32_t block_min_cells; /* pairs with n1*n2 >= this run one per CTA (0 = 2^22) */
-  int32_t reserved;
+  int64_t block_min_cells; /* pairs with n1*n2 >= this run one per CTA (0 = 2^22) */
+  int64_t long_min_cells;  /* pairs with n1*n2 >= this run on the plain path, many CTAs
+                            * each (0 = automatic: max(2^27, 8 x the batch's cells / CTAs),
+                            * so only a pair that even a team of 8 CTAs would take longer
+                            * on than an even share of the batch; -1 = never) */
+  int64_t team_min_cells;  /* pairs with n1*n2 >= this (and 4+ groups of bands) run on a
+                            * team of CTAs (0 = 2^25; -1 = never) */
 } gme_batch_config;
 
 gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg);
@@ -163,9 +170,77 @@ gme_status gme_batch_plan_run(gme_batch_plan *plan, const int32_t *d_symbols,
                               int use_graph);
 gme_status gme_batch_plan_destroy(gme_batch_plan *plan);
 
-/* How the last batch (or last plan made) was split: one-per-CTA, one-per-warp and plain-path pairs. */
+/* How the last batch (or last plan made) was split: one-per-CTA, one-per-warp,
+ * plain-path and team pairs (any pointer may be NULL). */
 gme_status gme_batch_stats(const gme_context *ctx, int64_t *block_jobs, int64_t *warp_jobs,
-                           int64_t *long_jobs);
+                           int64_t *long_jobs, int64_t *team_jobs);
+
+/* ---- served path: requests one at a time, each result as soon as it is done ----
+ * A server owns a host request queue, a dispatcher thread and `waves` launch slots
+ * (each a stream with its own device buffers).  gme_submit copies a request into
+ * the queue and returns a ticket at once.  The dispatcher admits queued requests
+ * in arrival order against the HBM budget, packs them into the next free slot
+ * (symbols in one copy from pinned memory) and launches the batched work-queue
+ * kernel there; the kernel writes each result and then its completion flag into
+ * pinned host memory, so a request completes when its own pair is done, not when
+ * its launch is.  Slots run concurrently: a new launch's CTAs take over SMs as the
+ * previous launch drains.  No counterpart in the reference, whose host functions
+ * align one pair per call (EditDistance/GPU_Hyperlane_Share.cu:689-789). */
+typedef struct gme_server gme_server;
+typedef struct gme_server_config {
+  int64_t hbm_budget_bytes; /* device memory the server may hold in all (0 = 20 GiB) */
+  int64_t wave_max_cells;   /* cells per launch at most (0 = 2^33) */
+  int32_t waves;            /* launch slots = launches in flight at once (0 = 3) */
+  int32_t queue_max;        /* requests the host queue holds (0 = 2^20) */
+  int32_t warps_per_block;  /* batch kernel CTA shape, 4 or 8 (0 = automatic) */
+  int32_t reserved;
+} gme_server_config;
+
+typedef struct gme_server_stats {
+  int64_t submitted, completed; /* requests */
+  int64_t queued, running;      /* waiting on the host; admitted to a launch */
+  int64_t waves_launched;       /* launches of the batched kernel sequence */
+  int64_t kernels_launched;     /* CUDA kernels, all slots */
+  int64_t cells_completed;      /* sum of n1*n2 over completed requests */
+  int64_t hbm_bytes_held;       /* device memory held by the server now */
+  int64_t hbm_bytes_peak;       /* ... and at most so far */
+  int64_t hbm_budget_bytes;
+  int64_t h2d_bytes;            /* symbols and descriptors copied to the device */
+  int64_t d2h_bytes;            /* results and flags the device wrote to host memory */
+} gme_server_stats;
+
+/* One scoring for every request of the server (as for a batch). */
+gme_status gme_server_create(int device, const gme_server_config *cfg, const gme_scoring *sc,
+                             gme_server **out);
+/* Stops admitting, lets the launches in flight finish, completes what is still
+ * queued with status GME_ERR_CLOSED, joins the dispatcher and frees everything. */
+gme_status gme_server_destroy(gme_server *s);
+/* Queues one alignment; a and b are copied, so they may be reused at once.  Never
+ * waits for the GPU.  GME_ERR_BUDGET: the request alone needs more device memory
+ * than one slot's share of the budget.  GME_ERR_NOT_READY: the queue is full. */
+gme_status gme_submit(gme_server *s, gme_kind kind, const int32_t *a, int64_t n1, const int32_t *b,
+                      int64_t n2, uint64_t *ticket);
+/* Queues n alignments in one call: request i reads symbols as batch pair i does
+ * (kind, a_off/n1, b_off/n2) and gets its own ticket tickets[i].  The same errors
+ * as gme_submit; on one, the requests before it stay queued and *submitted says
+ * how many there are. */
+gme_status gme_submit_many(gme_server *s, const int32_t *symbols, const gme_pair *pairs, int64_t n,
+                           uint64_t *tickets, int64_t *submitted);
+/* GME_OK with *out (and *latency_ns, submission to completion; may be NULL) once
+ * the request is done; the ticket is then forgotten.  GME_ERR_NOT_READY while it
+ * is queued or running; GME_ERR_INVALID for a ticket never issued or already
+ * taken.  out->status carries the request's own status. */
+gme_status gme_poll(gme_server *s, uint64_t ticket, gme_result *out, int64_t *latency_ns);
+/* Takes up to `max` finished requests in completion order.  results and
+ * latency_ns may be NULL; *count gets the number taken. */
+gme_status gme_poll_many(gme_server *s, uint64_t *tickets, gme_result *results,
+                         int64_t *latency_ns, int64_t max, int64_t *count);
+/* Blocks until every request submitted so far has completed; GME_ERR_NOT_READY
+ * if timeout_ns passes first. */
+gme_status gme_server_drain(gme_server *s, uint64_t timeout_ns);
+gme_status gme_server_get_stats(const gme_server *s, gme_server_stats *out);
+/* Text of the last error the server met (never NULL). */
+const char *gme_server_last_error(const gme_server *s);
 
 /* ---- plain path without allocation --------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc (code
