@@ -422,8 +422,8 @@ gme_status gme_server_create(int device, const gme_server_config *cfg, const gme
       (c.warps_per_block && c.warps_per_block != 4 && c.warps_per_block != 8))
     return GME_ERR_INVALID;
   if (!c.hbm_budget_bytes) c.hbm_budget_bytes = 20ll << 30;
-  if (!c.wave_max_cells) c.wave_max_cells = 1ll << 33;
-  if (!c.waves) c.waves = 3;
+  if (!c.wave_max_cells) c.wave_max_cells = 1ll << 35;
+  if (!c.waves) c.waves = 4;
   if (!c.queue_max) c.queue_max = 1 << 20;
   if (c.waves > 16) return GME_ERR_INVALID;
   gme_scoring s0 = gme_default_scoring();

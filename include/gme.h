@@ -189,8 +189,8 @@ gme_status gme_batch_stats(const gme_context *ctx, int64_t *block_jobs, int64_t 
 typedef struct gme_server gme_server;
 typedef struct gme_server_config {
   int64_t hbm_budget_bytes; /* device memory the server may hold in all (0 = 20 GiB) */
-  int64_t wave_max_cells;   /* cells per launch at most (0 = 2^33) */
-  int32_t waves;            /* launch slots = launches in flight at once (0 = 3) */
+  int64_t wave_max_cells;   /* cells per launch at most (0 = 2^35) */
+  int32_t waves;            /* launch slots = launches in flight at once (0 = 4) */
   int32_t queue_max;        /* requests the host queue holds (0 = 2^20) */
   int32_t warps_per_block;  /* batch kernel CTA shape, 4 or 8 (0 = automatic) */
   int32_t reserved;
