@@ -43,6 +43,18 @@ METRIC = "GCUPS on 1 GB300, batched/served vs plain per-pair (bit-exact); p50/p9
 L2_FLUSH_BYTES = 256 << 20
 
 
+def profiled_traffic(name: str):
+    """DRAM bytes per launch of the dominant kernel, from the committed ncu summary
+    (`dram_bytes_per_launch: N` in profiles/<name>.md), or None."""
+    import re
+    try:
+        txt = open(os.path.join(REPO, "profiles", name + ".md")).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*(\d+)", txt)
+    return int(m.group(1)) if m else None
+
+
 def workload(name: str):
     from gpumemefficient_gb300 import synth
     if name == "ed65536":
@@ -291,9 +303,13 @@ def run_gme(args):
     mean_s = t_dev / args.steps
     achieved = cells * OPS_PER_CELL[kind] / mean_s / 1e12
     roof = {"bound": "int_alu", "achieved": achieved, "peak": peak_tops, "unit": "Tops/s",
-            "frac": achieved / peak_tops, "traffic": None,
+            "frac": achieved / peak_tops,
+            "traffic": profiled_traffic("plain_kernel_ed65536") if args.workload == "ed65536" else None,
+            "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one launch, ncu capture in "
+                            "profiles/plain_kernel_ed65536.md",
             "peak_basis": f"{sms} SMs x {INT_LANES_PER_SM} INT32 lanes x median SM clock "
-                          f"{mhz:.0f} MHz under load ({'measured' if clk.get('sm_mhz') else 'assumed'})",
+                          f"{mhz:.0f} MHz under load ({'measured' if clk.get('sm_mhz') else 'assumed'}); "
+                          "MEASURED_PEAKS.json has no integer figure",
             "ops_per_cell": OPS_PER_CELL[kind], "kernel": "plain_kernel (whole step timed)"}
 
     cpu = cpu_baseline(kind, a, b) if (rank == 0 and not args.no_cpu) else None
@@ -306,11 +322,10 @@ def run_gme(args):
             "data": "synthetic (seeded)", "config": cfg, "clocks": clk, "e2e": e2e,
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
             "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)}}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     ctx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+    return line if rank == 0 else None
 
 
 def run_gme_batch(args):
@@ -431,7 +446,10 @@ def run_gme_batch(args):
     peak_tops = sms * INT_LANES_PER_SM * mhz * 1e6 / 1e12
     achieved = ops / mean_s / 1e12
     roof = {"bound": "int_alu", "achieved": achieved, "peak": peak_tops, "unit": "Tops/s",
-            "frac": achieved / peak_tops, "traffic": None,
+            "frac": achieved / peak_tops,
+            "traffic": profiled_traffic("batch_kernel_batched16384") if n == 16384 else None,
+            "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one launch, ncu capture in "
+                            "profiles/batch_kernel_batched16384.md",
             "peak_basis": f"{sms} SMs x {INT_LANES_PER_SM} INT32 lanes x median SM clock {mhz:.0f} MHz under load",
             "ops_per_cell": "LCS 4, ED 7, SW 8 weighted by cells", "kernel": "batch_kernel (whole graph timed)"}
     cpu = None
@@ -455,12 +473,11 @@ def run_gme_batch(args):
             "data": "synthetic (seeded)", "config": cfg, "clocks": clk, "e2e": e2e,
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
             "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)}}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     plan.close()
     ctx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+    return line if rank == 0 else None
 
 
 def _percentiles(lat_ns):
@@ -660,17 +677,54 @@ def main():
     p.add_argument("--rate-seconds", type=float, default=2.0, help="served workload: seconds per rate point")
     p.add_argument("--wave-cells", type=int, default=0, help="served workload: cells per launch at most (0 = default)")
     p.add_argument("--no-parity", action="store_true", help="skip the oracle parity check (tuning runs)")
+    p.add_argument("--solo", action="store_true",
+                   help="default workload only (no batched/served summaries beside it)")
     args = p.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload == "batched":
-        run_gme_batch(args)
+        return
+    if args.workload == "batched":
+        line = run_gme_batch(args)
     elif args.workload == "served":
-        print(json.dumps(run_gme_served(args)), flush=True)
+        line = run_gme_served(args)
     else:
-        run_gme(args)
+        line = run_gme(args)
+        ws = dist_env()[0]
+        if line is not None and args.workload == "ed65536" and ws == 1 and not args.solo:
+            line["also"] = also_batched_served(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def also_batched_served(args):
+    """Short runs of the batched and served workloads, summarised beside the headline
+    line (the metric compares batched/served with the plain per-pair path)."""
+    import copy
+    out = {}
+    a = copy.copy(args)
+    a.steps, a.warmup, a.no_cpu, a.pairs, a.batch_warps = 10, 3, True, 16384, 0
+    b = run_gme_batch(a)
+    c = b["config"]
+    out["batched"] = {"workload": c["workload"], "value": b["value"], "unit": "GCUPS",
+                      "ms_per_step": b["ms_per_step"], "e2e": b["e2e"]["value"],
+                      "plain_per_pair_gcups": c["plain_per_pair_gcups"],
+                      "batched_over_plain": c["batched_over_plain"], "split": c["split"],
+                      "parity_vs_oracle": c["parity_vs_oracle"], "roofline_frac": b["roofline"]["frac"],
+                      "gpu_launches": b["gpu_launches"], "clocks": b["clocks"]}
+    a = copy.copy(args)
+    a.steps, a.warmup, a.no_cpu, a.requests, a.waves, a.wave_cells = 3, 3, True, 8192, 0, 0
+    a.rates, a.rate_seconds, a.no_parity = [0.1, 0.5, 0.8], 1.5, False
+    s = run_gme_served(a)
+    c = s["config"]
+    out["served"] = {"workload": c["workload"], "value": s["value"], "unit": "GCUPS",
+                     "batched_same_requests_gcups": c["batched_same_requests_gcups"],
+                     "served_over_batched": c["served_over_batched"], "rate_sweep": c["rate_sweep"],
+                     "parity_vs_oracle": c["parity_vs_oracle"], "hbm_bytes_peak": c["hbm_bytes_peak"],
+                     "hbm_budget_bytes": c["hbm_budget_bytes"], "gpu_launches": s["gpu_launches"],
+                     "clocks": s["clocks"]}
+    return out
 
 
 if __name__ == "__main__":
