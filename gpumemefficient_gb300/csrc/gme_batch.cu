@@ -248,57 +248,55 @@ __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict_
   int ib[2][CB];
   bool ok_next = src_fetch<KIND>(in, 0, ib[0]);
 
-  auto chunk = [&](int j, auto par, auto checked, auto padrows) -> bool {
-    constexpr int PAR = decltype(par)::value;
+  // One chunk body per variant: the symbol window and the read-ahead buffer are
+  // shifted by register moves after each chunk (about two moves per step), instead
+  // of unrolling two window parities -- the loop then stays half as large in the
+  // instruction cache, which a dozen warps per SM at different points of their own
+  // pairs share.
+  auto chunk = [&](int j, auto checked, auto padrows) -> bool {
     constexpr bool CK = decltype(checked)::value, PD = decltype(padrows)::value;
-    int(&inv)[CB] = ib[PAR];
     const int s0 = CB * j;
     __syncwarp();
     if (s0 <= N && !__all_sync(FULL, ok_next)) {
-      if (!W.wait([&] { return __all_sync(FULL, src_fetch<KIND>(in, j, inv)); })) return false;
+      if (!W.wait([&] { return __all_sync(FULL, src_fetch<KIND>(in, j, ib[0])); })) return false;
     }
     // consumed: this chunk, but never past the end of this band's row -- the ring's
     // next positions already belong to the next band group of the same pair
     if (in.mode == IN_RING && lane == 31) sts_vol(in.cons, in.base + min(s0 + CB, row_end));
-    if (lane == 0) recv = inv[0];
-    ok_next = src_fetch<KIND>(in, j + 1, ib[PAR ^ 1]);
+    if (lane == 0) recv = ib[0][0];
+    ok_next = src_fetch<KIND>(in, j + 1, ib[1]);
     int outq[CB];
-    steps_chunk<KIND, R, PAR, CK, PD, CB>(rec, cur, prv, recv, recv_prev, win, sym + s0 + CB, bs, inv,
-                                      outq, s0, lane, N, padmask, smax, sstep);
+    steps_chunk<KIND, R, 0, CK, PD, CB>(rec, cur, prv, recv, recv_prev, win, sym + s0 + CB, bs, ib[0],
+                                        outq, s0, lane, N, padmask, smax, sstep);
+    // the next chunk's symbols (loaded into the upper half at step R) move down;
+    // the last R-1 symbols of this chunk become the window's wrapped tail
+    int tail[R - 1];
+#pragma unroll
+    for (int d = 0; d < R - 1; ++d) tail[d] = win[CB - R + 1 + d];
+#pragma unroll
+    for (int k = 0; k < CB; ++k) win[k] = win[k + CB];
+#pragma unroll
+    for (int d = 0; d < R - 1; ++d) win[2 * CB - R + 1 + d] = tail[d];
+#pragma unroll
+    for (int k = 0; k < CB; ++k) ib[0][k] = ib[1][k];
     const int pos = s0 - 32 * R;
     if (pos >= 0 && !dst_put(out, pos, outq, lane, W)) return false;
     return true;
   };
 
+  // Two chunk bodies, each instantiated once: the steady one, and one that both
+  // holds out-of-range cells and passes padding rows through (ramps, last band).
   using T = std::true_type;
   using F = std::false_type;
-  using P0 = std::integral_constant<int, 0>;
-  using P1 = std::integral_constant<int, 1>;
-  auto range = [&](int ja, int jb, auto ck, auto pd) -> bool {
-    int j = ja;
-    if (j <= jb && (j & 1)) {
-      if (!chunk(j, P1{}, ck, pd)) return false;
-      ++j;
-    }
-    for (; j + 1 <= jb; j += 2) {
-      if (!chunk(j, P0{}, ck, pd)) return false;
-      if (!chunk(j + 1, P1{}, ck, pd)) return false;
-    }
-    if (j <= jb && !chunk(j, P0{}, ck, pd)) return false;
-    return true;
-  };
-  // Two chunk bodies per parity keep the code small (the instruction cache is
-  // shared by every kind in flight on an SM): the steady one, and one that both
-  // holds out-of-range cells and passes padding rows through (ramps, last band).
   const int j_end = (N + 32 * R) / CB;
-  if (padwarp) {
-    if (!range(0, j_end, T{}, T{})) return false;
-  } else {
-    const int j_lo = min((32 * R) / CB, j_end + 1);
-    const int j_hi = max(min((N - CB + 1) / CB, j_end), j_lo - 1);
-    if (!range(0, j_lo - 1, T{}, T{})) return false;
-    if (!range(j_lo, j_hi, F{}, F{})) return false;
-    if (!range(j_hi + 1, j_end, T{}, T{})) return false;
+  const int j_lo = padwarp ? j_end + 1 : min((32 * R) / CB, j_end + 1);
+  const int j_hi = padwarp ? j_end : max(min((N - CB + 1) / CB, j_end), j_lo - 1);
+  for (int j = 0; j <= j_end; ++j) {
+    if (j >= j_lo && j <= j_hi) {
+      if (!chunk(j, F{}, F{})) return false;
+    } else {
+      if (!chunk(j, T{}, T{})) return false;
+    }
   }
   corner = cur[R - 1];
 #pragma unroll
