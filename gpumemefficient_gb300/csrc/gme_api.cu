@@ -441,6 +441,9 @@ gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg) {
     t.long_min_cells = cfg->long_min_cells;
     if (cfg->team_min_cells) t.team_min_cells = cfg->team_min_cells;
   }
+  // an all-zero configuration means "automatic" (the tuned table)
+  t.user_set = cfg && (cfg->warps_per_block || cfg->blocks_per_sm || cfg->block_min_cells ||
+                       cfg->long_min_cells || cfg->team_min_cells);
   ctx->batch_tune = t;
   return GME_OK;
 }

@@ -15,12 +15,14 @@
 // functions (EditDistance/GPU_Hyperlane_Share.cu:689-789 and its LCS/SW twins).
 #include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstring>
 #include <numeric>
 #include <vector>
 
 #include "gme_engine.cuh"
 #include "gme_internal.h"
+#include "gme_tuned.h"
 
 namespace gme {
 
@@ -634,9 +636,37 @@ long long batch_scratch_bytes(long long grid, int NW, int max_n1) {
 // The plan: classify the pairs (per warp, per CTA, or plain path), order them
 // longest first, lay the staged symbols out and upload the descriptors.  Waits
 // for the arena's previous work on `st` before reusing its buffers.
+// The settings a batch is planned with: the caller's, or the tuned entry whose
+// length range is nearest (in log scale) to the batch's own, taken as the 2nd and
+// 98th percentiles of sqrt(n1*n2) over its pairs.
+BatchTuning batch_tuning_for(const gme_pair *pairs, long long npairs, const BatchTuning &given) {
+  if (given.user_set || TUNED_BUCKETS == 0 || npairs == 0) return given;
+  std::vector<float> len((size_t)npairs);
+  for (long long i = 0; i < npairs; ++i)
+    len[i] = std::sqrt((float)pairs[i].n1 * (float)pairs[i].n2) + 1.0f;
+  const size_t i_lo = (size_t)(0.02 * (npairs - 1)), i_hi = (size_t)(0.98 * (npairs - 1));
+  std::nth_element(len.begin(), len.begin() + i_lo, len.end());
+  const float lo = len[i_lo];
+  std::nth_element(len.begin(), len.begin() + i_hi, len.end());
+  const float hi = len[i_hi];
+  int best = 0;
+  float best_d = 1e30f;
+  for (int b = 0; b < TUNED_BUCKETS; ++b) {
+    const float d = std::fabs(std::log(lo / (float)TUNED[b].lo)) + std::fabs(std::log(hi / (float)TUNED[b].hi));
+    if (d < best_d) { best_d = d; best = b; }
+  }
+  BatchTuning t = given;
+  t.warps_per_block = TUNED[best].warps_per_block;
+  t.blocks_per_sm = TUNED[best].blocks_per_sm;
+  t.block_min_cells = TUNED[best].block_min_cells;
+  t.team_min_cells = TUNED[best].team_min_cells;
+  return t;
+}
+
 int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long npairs,
-               long long nsym, const BatchTuning &tune, cudaStream_t st) {
+               long long nsym, const BatchTuning &tune_given, cudaStream_t st) {
   constexpr int R = 4;
+  const BatchTuning tune = batch_tuning_for(pairs, npairs, tune_given);
   const int NW = tune.warps_per_block;
   if (!batch_config_valid(NW)) return ws.fail_msg(ST_INVALID, "batch: warps_per_block must be 4 or 8");
   std::vector<int> blockj, warpj, teamj;

@@ -57,6 +57,9 @@ struct BatchTuning {
   long long long_min_cells = 0;
   // pairs at least this large (with 4+ band groups) run on a team of CTAs; < 0 = never
   long long team_min_cells = 1ll << 25;
+  // false: the plan takes warps, CTAs per SM and cut-offs from the tuned table
+  // (gme_tuned.h) for the batch's length bucket
+  bool user_set = false;
 };
 
 // Device and host buffers of the batched path, owned by a context, grown on demand.

@@ -83,8 +83,8 @@ struct gme_server {
   gme_scoring sc{};
   gme_server_config cfg{};
   int64_t wave_bytes = 0;  // device bytes one launch may add (a third of a slot's share)
-  int NW = 4;              // batch kernel CTA shape
-  long long grid = 0;      // its CTAs
+  int NW = 0;              // batch kernel CTA shape (0: the tuned table's choice)
+  long long grid4 = 0, grid8 = 0;  // the kernel's CTAs at 4 and 8 warps per CTA
   std::vector<Slot> slots;
   std::thread dispatcher;
 
@@ -105,6 +105,13 @@ namespace {
 void set_error(gme_server *s, const std::string &m) {
   std::lock_guard<std::mutex> g(s->mu);
   s->last_error = m;
+}
+
+// Per-CTA rows of a launch whose widest pair is max_n1 wide, at the CTA shape the
+// launch may take.
+int64_t scratch_bytes(const gme_server *s, int max_n1) {
+  if (s->NW) return gme::batch_scratch_bytes(s->NW == 8 ? s->grid8 : s->grid4, s->NW, max_n1);
+  return std::max(gme::batch_scratch_bytes(s->grid4, 4, max_n1), gme::batch_scratch_bytes(s->grid8, 8, max_n1));
 }
 
 int64_t held_bytes(const gme_server *s) {
@@ -219,7 +226,7 @@ bool launch(gme_server *s, Slot &sl) {
       const int64_t c = (int64_t)q.n1 * q.n2;
       const int mn = std::max(max_n1, std::min(q.n1, gme::BATCH_MAX_N1));
       const int64_t b = bytes + q.bytes;
-      const int64_t fixed = gme::batch_scratch_bytes(s->grid, s->NW, mn);
+      const int64_t fixed = scratch_bytes(s, mn);
       if (!sl.reqs.empty() && (cells + c > s->cfg.wave_max_cells || b + fixed > s->wave_bytes)) break;
       cells += c;
       bytes = b;
@@ -372,7 +379,7 @@ gme_status make_request(gme_server *s, int kind, const int32_t *a, int64_t n1, c
   // workspace holds both padded sequences and a boundary row per band
   q.bytes = gme::batch_pair_bytes(n1, n2) + (n1 > gme::BATCH_MAX_N1 ? 64 * (n1 + n2) + (1 << 20) : 0);
   // alone in a launch it brings the per-CTA rows for its width
-  const int64_t fixed = gme::batch_scratch_bytes(s->grid, s->NW, (int)std::min<int64_t>(n1, gme::BATCH_MAX_N1));
+  const int64_t fixed = scratch_bytes(s, (int)std::min<int64_t>(n1, gme::BATCH_MAX_N1));
   if (q.bytes + fixed > s->wave_bytes) return GME_ERR_BUDGET;
   q.sym.resize((size_t)(n1 + n2));
   if (n1) std::memcpy(q.sym.data(), a, (size_t)n1 * 4);
@@ -440,9 +447,11 @@ gme_status gme_server_create(int device, const gme_server_config *cfg, const gme
   gme_status rc = GME_OK;
   for (Slot &sl : s->slots) {
     if ((rc = gme_create(device, &sl.ctx)) != GME_OK) break;
-    gme_batch_config bc{};
-    bc.warps_per_block = c.warps_per_block;
-    if ((rc = gme_set_batch_config(sl.ctx, &bc)) != GME_OK) break;
+    if (c.warps_per_block) {
+      gme_batch_config bc{};
+      bc.warps_per_block = c.warps_per_block;
+      if ((rc = gme_set_batch_config(sl.ctx, &bc)) != GME_OK) break;
+    }
     sl.st = gme::ctx_stream(sl.ctx);
     if (cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess) {
       rc = GME_ERR_CUDA;
@@ -450,8 +459,9 @@ gme_status gme_server_create(int device, const gme_server_config *cfg, const gme
     }
   }
   if (rc == GME_OK) {
-    s->NW = c.warps_per_block ? c.warps_per_block : 4;
-    s->grid = gme::batch_grid(gme::ctx_sms(s->slots[0].ctx), s->NW, 0);
+    s->NW = c.warps_per_block;
+    s->grid4 = gme::batch_grid(gme::ctx_sms(s->slots[0].ctx), 4, 0);
+    s->grid8 = gme::batch_grid(gme::ctx_sms(s->slots[0].ctx), 8, 0);
   }
   if (rc != GME_OK) {
     for (Slot &sl : s->slots) {

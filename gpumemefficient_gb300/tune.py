@@ -1,0 +1,227 @@
+"""Autotuner of the batched kernel.
+
+Sweeps, per length bucket, the launch shape and the job-class cut-offs of the
+batched work-queue kernel:
+
+* warps per CTA (the CTA's tile: warps_per_block x 32 lanes x 4 rows of a band group),
+* CTAs per SM,
+* block_min_cells (pairs at least this large run one per CTA, the rest one per warp),
+* team_min_cells (pairs at least this large run on a team of CTAs),
+
+on seeded synthetic batches whose lengths are log-uniform within the bucket (LCS,
+ED and SW one third each), timing CUDA-graph replays of one planned launch with CUDA
+events.  Every configuration is checked bit-exact against the first one's results
+(which the batched tests pin to the oracle).
+
+    python -m gpumemefficient_gb300.tune [--out-json F] [--out-md F] [--quick]
+
+writes the whole sweep (`--out-md`, a table) and the winners per bucket
+(`--out-json`).  `gen_header()` (or `--header`, or `header_from_json()` on a
+committed result) turns the winners into `csrc/gme_tuned.h`, the table the
+library's batch plan consults when the caller has not set a batch configuration
+(gme_set_batch_config): the entry whose length range is nearest the batch's.
+"""
+from __future__ import annotations
+
+import argparse
+import itertools
+import json
+import os
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+TUNED_JSON = os.path.join(HERE, "tuned.json")
+TUNED_H = os.path.join(HERE, "csrc", "gme_tuned.h")
+
+# (name, shortest, longest length); the buckets tile the lengths the batch kernel takes
+BUCKETS = [
+    ("short", 32, 512),
+    ("mid", 512, 2048),
+    ("long", 2048, 8192),
+    ("wide", 8192, 16384),
+]
+# the two benchmark distributions, tuned and reported beside the buckets
+MIXES = [
+    ("mixed_64_4096", 64, 4096),
+    ("mixed_32_16384", 32, 16384),
+]
+
+GRID = {
+    "warps_per_block": [4, 8],
+    "blocks_per_sm": [0, 2],
+    "block_min_cells": [1 << 20, 1 << 21, 1 << 22, 1 << 23],
+    "team_min_cells": [1 << 24, 1 << 25, 1 << 26, -1],
+}
+QUICK_GRID = {
+    "warps_per_block": [4, 8],
+    "blocks_per_sm": [0],
+    "block_min_cells": [1 << 21, 1 << 22],
+    "team_min_cells": [1 << 25, -1],
+}
+
+
+def batch_for(lo: int, hi: int, cells: float, seed: int):
+    """Seeded pairs with lengths log-uniform in [lo, hi] until about `cells` cells."""
+    from . import pack_batch
+    rng = np.random.default_rng(seed)
+    mean = ((hi - lo) / np.log(hi / lo)) ** 2
+    n = int(min(40000, max(64, cells / mean)))
+    la = np.exp(rng.uniform(np.log(lo), np.log(hi), n)).astype(np.int64)
+    lb = np.exp(rng.uniform(np.log(lo), np.log(hi), n)).astype(np.int64)
+    kinds = np.repeat(np.arange(3, dtype=np.int32), (n + 2) // 3)[:n]
+    rng.shuffle(kinds)
+    sa = [rng.integers(0, 4, int(k), dtype=np.int64).astype(np.int32) for k in la]
+    sb = [rng.integers(0, 4, int(k), dtype=np.int64).astype(np.int32) for k in lb]
+    symbols, pairs = pack_batch(kinds, sa, sb)
+    return symbols, pairs, float((la * lb).sum())
+
+
+def measure(ctx, d_sym, d_res, pairs, nsym, cfg, reps, stream):
+    """GCUPS of one configuration (graph replays timed with CUDA events) and its results."""
+    import torch
+    from . import BatchPlan, RESULT_DTYPE
+    ctx.set_batch_config(**cfg)
+    plan = BatchPlan(ctx, pairs, nsym)
+    split = ctx.batch_stats()
+    sp = stream.cuda_stream
+    try:
+        for _ in range(2):
+            plan.run(d_sym.data_ptr(), d_res.data_ptr(), stream=sp, use_graph=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            plan.run(d_sym.data_ptr(), d_res.data_ptr(), stream=sp, use_graph=True)
+        e1.record(stream)
+        stream.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+    finally:
+        plan.close()
+        ctx.set_batch_config()
+    res = np.frombuffer(d_res.cpu().numpy().tobytes(), RESULT_DTYPE).copy()
+    return ms, split, res
+
+
+def sweep(grid=None, cells: float = 1.5e10, reps: int = 5, device: int = 0, log=print):
+    import torch
+    from . import Context, RESULT_DTYPE
+    grid = grid or GRID
+    keys = list(grid)
+    ctx = Context(device)
+    dev = torch.device("cuda", device)
+    stream = torch.cuda.Stream(device=device)
+    rows = []
+    for bi, (name, lo, hi) in enumerate(BUCKETS + MIXES):
+        symbols, pairs, total = batch_for(lo, hi, cells, 0x5EED + bi)
+        d_sym = torch.from_numpy(symbols).to(dev)
+        d_res = torch.zeros(len(pairs) * RESULT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+        ref = None
+        for vals in itertools.product(*(grid[k] for k in keys)):
+            cfg = dict(zip(keys, vals))
+            ms, split, res = measure(ctx, d_sym, d_res, pairs, len(symbols), cfg, reps, stream)
+            ok = bool((res["status"] == 0).all())
+            if ref is None:
+                ref = res
+            same = bool((res["score"] == ref["score"]).all() and (res["sw_max"] == ref["sw_max"]).all())
+            row = {"bucket": name, "lo": lo, "hi": hi, "pairs": len(pairs), "cells": total, **cfg,
+                   "ms": ms, "gcups": total / ms / 1e6, "split": split, "ok": ok and same}
+            rows.append(row)
+            log(json.dumps(row))
+        del d_sym, d_res
+    ctx.close()
+    return rows
+
+
+def winners(rows):
+    best = {}
+    for r in rows:
+        if not r["ok"]:
+            continue
+        b = best.get(r["bucket"])
+        if b is None or r["gcups"] > b["gcups"]:
+            best[r["bucket"]] = r
+    return best
+
+
+def write_md(rows, best, path, cmd):
+    keys = ["warps_per_block", "blocks_per_sm", "block_min_cells", "team_min_cells"]
+    lines = ["# Batched-kernel autotune sweep", "",
+             f"Command (GB300): `{cmd}`", "",
+             "GCUPS of one planned launch (CUDA-graph replay, CUDA events, mean of the replays) "
+             "per length bucket; lengths log-uniform in [lo, hi], LCS/ED/SW one third each. "
+             "`team_min_cells` -1 = no teams. Every row's results equal the first row's.", ""]
+    for name in [b[0] for b in BUCKETS + MIXES]:
+        rs = [r for r in rows if r["bucket"] == name]
+        if not rs:
+            continue
+        w = best.get(name)
+        lines.append(f"## {name}: lengths [{rs[0]['lo']}, {rs[0]['hi']}], {rs[0]['pairs']} pairs, "
+                     f"{rs[0]['cells']:.3g} cells")
+        lines.append("")
+        lines.append("| warps/CTA | CTAs/SM | block_min | team_min | ms | GCUPS | split (team/block/warp/plain) | |")
+        lines.append("|---:|---:|---:|---:|---:|---:|---|---|")
+        for r in sorted(rs, key=lambda r: -r["gcups"]):
+            s = r["split"]
+            mark = "best" if r is w else ("" if r["ok"] else "MISMATCH")
+            lines.append(f"| {r['warps_per_block']} | {r['blocks_per_sm'] or 'max'} | 2^{int(np.log2(r['block_min_cells']))} | "
+                         f"{('2^%d' % int(np.log2(r['team_min_cells']))) if r['team_min_cells'] > 0 else 'none'} | "
+                         f"{r['ms']:.3f} | {r['gcups']:.1f} | {s.get('team_jobs', 0)}/{s['block_jobs']}/{s['warp_jobs']}/{s['long_jobs']} | {mark} |")
+        lines.append("")
+    with open(path, "w") as f:
+        f.write("\n".join(lines))
+
+
+def gen_header(best, path=TUNED_H):
+    """The winners per bucket (and per mix) as the table the batch plan reads."""
+    keys = [b for b in BUCKETS + MIXES if b[0] in best]
+    out = ["// gme_tuned.h -- batched-kernel settings per length range, written by",
+           "// gpumemefficient_gb300/tune.py from a sweep on GB300 (the sweep table is kept",
+           "// beside the profiles).  A batch is planned with the entry whose length range",
+           "// [lo, hi] is nearest (in log scale) to the batch's own: the 2nd..98th",
+           "// percentile of sqrt(n1*n2) over its pairs -- unless the caller set its own.",
+           "#pragma once", "", "namespace gme {", "",
+           "struct TunedBucket {", "  int lo, hi;", "  int warps_per_block, blocks_per_sm;",
+           "  long long block_min_cells, team_min_cells;", "};", "",
+           f"constexpr int TUNED_BUCKETS = {len(keys)};",
+           "constexpr TunedBucket TUNED[TUNED_BUCKETS > 0 ? TUNED_BUCKETS : 1] = {"]
+    for name, lo, hi in keys:
+        r = best[name]
+        out.append(f"    {{{lo}, {hi}, {r['warps_per_block']}, {r['blocks_per_sm']}, {r['block_min_cells']}ll, "
+                   f"{r['team_min_cells']}ll}},  // {name}: {r['gcups']:.0f} GCUPS")
+    if not keys:
+        out.append("    {0, 0, 4, 0, 1ll << 22, 1ll << 25},")
+    out += ["};", "", "}  // namespace gme", ""]
+    with open(path, "w") as f:
+        f.write("\n".join(out))
+
+
+def header_from_json(path=TUNED_JSON):
+    """Regenerates csrc/gme_tuned.h from a committed sweep result."""
+    gen_header(json.load(open(path))["best"])
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--out-json", default=TUNED_JSON)
+    p.add_argument("--out-md", default=None)
+    p.add_argument("--quick", action="store_true")
+    p.add_argument("--cells", type=float, default=1.5e10)
+    p.add_argument("--reps", type=int, default=5)
+    p.add_argument("--header", action="store_true", help="also regenerate csrc/gme_tuned.h")
+    a = p.parse_args()
+    t0 = time.time()
+    rows = sweep(QUICK_GRID if a.quick else GRID, a.cells, a.reps)
+    best = winners(rows)
+    with open(a.out_json, "w") as f:
+        json.dump({"best": best, "rows": rows, "seconds": time.time() - t0}, f, indent=1)
+    if a.out_md:
+        write_md(rows, best, a.out_md, "python -m gpumemefficient_gb300.tune" + (" --quick" if a.quick else "")
+                 + f" --out-md {a.out_md}")
+    if a.header:
+        gen_header(best)
+    print(json.dumps({k: {"gcups": v["gcups"], **{kk: v[kk] for kk in GRID}} for k, v in best.items()}))
+
+
+if __name__ == "__main__":
+    main()
