@@ -45,6 +45,7 @@ def up_to_date() -> bool:
 
 def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     if not force and up_to_date():
+        build_tools()
         return LIB
     os.makedirs(OUTDIR, exist_ok=True)
     cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -72,7 +73,34 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_tools()
     return LIB
+
+
+TOOLS = os.path.join(HERE, "tools")
+TOOL_BINS = {"gme-align": ("gme_align.cpp", True), "gme-generate": ("gme_generate.cpp", False)}
+
+
+def build_tools() -> dict:
+    """The command-line tools (host C++): gme-align (the reference's drivers on the
+    library) and gme-generate (the reference's data files from a seeded PRNG)."""
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    out = {}
+    for name, (src, uses_lib) in TOOL_BINS.items():
+        exe = os.path.join(OUTDIR, name)
+        deps = [os.path.join(TOOLS, src), os.path.join(TOOLS, "gme_datafile.h"),
+                os.path.join(REPO, "include", "gme.h")] + ([LIB] if uses_lib else [])
+        if not (os.path.exists(exe) and all(os.path.getmtime(d) <= os.path.getmtime(exe) for d in deps)):
+            cmd = [shutil.which("g++") or "g++", "-O2", "-std=c++17", "-I" + os.path.join(REPO, "include"),
+                   "-I" + TOOLS, os.path.join(TOOLS, src), "-o", exe + f".tmp{os.getpid()}"]
+            if uses_lib:
+                cmd += ["-L" + OUTDIR, "-lgme", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"{name} failed:\n{r.stdout}\n{r.stderr}")
+            os.replace(exe + f".tmp{os.getpid()}", exe)
+        out[name] = exe
+    return out
 
 
 if __name__ == "__main__":

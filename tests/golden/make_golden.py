@@ -101,6 +101,8 @@ def main():
     kat = {"source": "reference CPU programs LCS.cpp / ED.cpp / SW.cpp, unmodified, g++ -O2",
            "fixture": "fixture_2_15.bin (prefixes of length n of both sequences)",
            "fixture_sha256": hashlib.sha256(blob).hexdigest(),
+           "fixture_text_sha256": hashlib.sha256(open(os.path.join(DATA, "str1_2_15_str2_2_15.txt"), "rb").read()).hexdigest(),
+           "fixture_text": "sha256 of LCS/Data/str1_2_15_str2_2_15.txt as shipped (the text layout the data-file tools read and write)",
            "gpu_log_pin": {"n": 32768, "lcs": 21469, "source": "LCS/GPU_Hyperlane_Share.txt:102"},
            "cases": []}
     for k in range(8, 16):
