@@ -350,8 +350,8 @@ def run_gme_batch(args):
     cells = float(cells_k.sum())
     ops = float(sum(cells_k[np.asarray(kinds) == k].sum() * OPS_PER_CELL[k] for k in range(3)))
     ctx = g.Context(local)
-    if args.batch_warps:
-        ctx.set_batch_config(warps_per_block=args.batch_warps)
+    if args.batch_warps or args.int32:
+        ctx.set_batch_config(warps_per_block=args.batch_warps, packed16=-1 if args.int32 else 0)
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=local)
     sp = stream.cuda_stream
@@ -469,7 +469,8 @@ def run_gme_batch(args):
            "batched_over_plain": value / ws / plain_gcups}
     line = {"metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * mean_s,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32" if args.int32 else "int16x2 (pairs whose scores fit 16 bits) / int32",
             "data": "synthetic (seeded)", "config": cfg, "clocks": clk, "e2e": e2e,
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
             "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)}}
@@ -670,6 +671,9 @@ def main():
     p.add_argument("--plain-sample", type=int, default=256,
                    help="batched workload: pairs timed one by one on the plain path")
     p.add_argument("--batch-warps", type=int, default=0, help="batched workload: warps per CTA")
+    p.add_argument("--int32", action="store_true",
+                   help="batched workload: every pair on the int32 engine (default: pairs that fit "
+                        "16 bits on the packed s16x2 engine)")
     p.add_argument("--requests", type=int, default=8192, help="served workload: requests per step")
     p.add_argument("--waves", type=int, default=0, help="served workload: launch slots (0 = default)")
     p.add_argument("--rates", type=float, nargs="*", default=[0.1, 0.5, 0.8],
@@ -704,7 +708,7 @@ def also_batched_served(args):
     import copy
     out = {}
     a = copy.copy(args)
-    a.steps, a.warmup, a.no_cpu, a.pairs, a.batch_warps = 10, 3, True, 16384, 0
+    a.steps, a.warmup, a.no_cpu, a.pairs, a.batch_warps, a.int32 = 10, 3, True, 16384, 0, False
     b = run_gme_batch(a)
     c = b["config"]
     out["batched"] = {"workload": c["workload"], "value": b["value"], "unit": "GCUPS",

@@ -82,14 +82,15 @@ int BatchArena::reserve(long long staged, long long nseg, long long njobs, Works
   int rc;
   if ((rc = grow_ll((void **)&d_staged, &staged_cap, staged, sizeof(int), ws, "cudaMalloc(batch staged)"))) return rc;
   if (seg_cap < nseg || !d_from) {
-    long long c0 = seg_cap, c1 = seg_cap, c2 = seg_cap, c3 = seg_cap, c4 = seg_cap;
+    long long c0 = seg_cap, c1 = seg_cap, c2 = seg_cap, c3 = seg_cap, c4 = seg_cap, c5 = seg_cap;
     if ((rc = grow_ll((void **)&d_from, &c0, nseg, 8, ws, "cudaMalloc(batch from)")) ||
         (rc = grow_ll((void **)&d_to, &c1, nseg, 8, ws, "cudaMalloc(batch to)")) ||
         (rc = grow_ll((void **)&d_len, &c2, nseg, 4, ws, "cudaMalloc(batch len)")) ||
         (rc = grow_ll((void **)&d_padl, &c3, nseg, 4, ws, "cudaMalloc(batch padl)")) ||
-        (rc = grow_ll((void **)&d_total, &c4, nseg, 4, ws, "cudaMalloc(batch total)")))
+        (rc = grow_ll((void **)&d_total, &c4, nseg, 4, ws, "cudaMalloc(batch total)")) ||
+        (rc = grow_ll((void **)&d_symbad, &c5, nseg, 4, ws, "cudaMalloc(batch symbol check)")))
       return rc;
-    seg_cap = std::min(std::min(c0, c1), std::min(std::min(c2, c3), c4));
+    seg_cap = std::min(std::min(std::min(c0, c1), std::min(c2, c3)), std::min(c4, c5));
   }
   if ((rc = grow_ll((void **)&d_jobs, &jobs_cap, njobs, sizeof(BatchJob), ws, "cudaMalloc(batch jobs)"))) return rc;
   if (!d_ctrl) {
@@ -131,7 +132,8 @@ void BatchArena::release() {
   cudaFree(d_units); cudaFree(d_team);
   d_units = nullptr; d_team = nullptr; units_cap = team_cap = 0;
   cudaFree(d_staged); cudaFree(d_from); cudaFree(d_to); cudaFree(d_len); cudaFree(d_padl);
-  cudaFree(d_total); cudaFree(d_jobs); cudaFree(d_ctrl);
+  cudaFree(d_total); cudaFree(d_jobs); cudaFree(d_ctrl); cudaFree(d_symbad);
+  d_symbad = nullptr;
   d_staged = nullptr; d_from = d_to = nullptr; d_len = d_padl = d_total = nullptr; d_jobs = nullptr;
   d_ctrl = nullptr; staged_cap = seg_cap = jobs_cap = 0;
 }
@@ -440,10 +442,13 @@ gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg) {
     if (cfg->block_min_cells) t.block_min_cells = cfg->block_min_cells;
     t.long_min_cells = cfg->long_min_cells;
     if (cfg->team_min_cells) t.team_min_cells = cfg->team_min_cells;
+    if (cfg->packed16 < -1 || cfg->packed16 > 1) return GME_ERR_INVALID;
+    t.packed16 = cfg->packed16 >= 0;
   }
   // an all-zero configuration means "automatic" (the tuned table)
   t.user_set = cfg && (cfg->warps_per_block || cfg->blocks_per_sm || cfg->block_min_cells ||
                        cfg->long_min_cells || cfg->team_min_cells);
+  if (!t.user_set && cfg) t.packed16 = cfg->packed16 >= 0;
   ctx->batch_tune = t;
   return GME_OK;
 }
@@ -652,7 +657,7 @@ long long ctx_device_bytes(const gme_context *ctx) {
   const Workspace &w = ctx->ws;
   const BatchArena &b = ctx->batch;
   long long n = 4 * (w.a_pad_cap + w.b_pad_cap) + 8 * w.slots_cap + 32ll * w.best_cap + (w.ctrl ? 64 : 0);
-  n += 4 * (b.staged_cap + b.rows_cap) + 28 * b.seg_cap + (long long)sizeof(BatchJob) * b.jobs_cap +
+  n += 4 * (b.staged_cap + b.rows_cap) + 32 * b.seg_cap + (long long)sizeof(BatchJob) * b.jobs_cap +
        8 * b.wrap_cap + (b.d_gen ? 4 * 1025 : 0) + (b.d_ctrl ? 64 : 0) + 16 * b.units_cap + b.team_cap;
   n += 4 * (ctx->d_a_cap + ctx->d_b_cap + ctx->d_row_cap + ctx->d_col_cap + ctx->d_bsym_cap) +
        (long long)sizeof(gme_result) * (ctx->d_bres_cap + 1);

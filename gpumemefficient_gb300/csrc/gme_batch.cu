@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "gme_engine.cuh"
+#include "gme_engine16.cuh"
 #include "gme_internal.h"
 #include "gme_tuned.h"
 
@@ -62,6 +63,8 @@ struct BatchParams {
   unsigned long long *twrap;  // two tagged rows of `stride` words per team job (cleared likewise)
   gme_result *results;
   int *done;               // optional: done[index] = 1 once results[index] is written (system scope)
+  const int *symbad;       // per staged segment: 1 if a symbol lies outside [0, 32767]
+  int packed16;            // jobs that qualify take the packed 16-bit engine
   int *rows;               // warp jobs: one row of `stride` ints per warp of the grid (L2-resident)
   unsigned long long *wrap;  // block jobs: two tagged rows of `stride` words per CTA
   unsigned *gen;           // tags handed out to wrap rows so far (kept across launches)
@@ -312,6 +315,130 @@ __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict_
   return true;
 }
 
+// The same band sweep on the packed 16-bit engine (gme_engine16.cuh): taken, when
+// the batch asks for it, by a job whose values fit 16 bits and whose symbols lie in
+// [0, 32767].  Rings, rows and
+// results carry the same int32 values as the int32 sweep.
+template <int KIND>
+__device__ __noinline__ bool sweep_band16(const Scoring sc, const int *__restrict__ a_sym,
+                                          const int *__restrict__ b_sym, int N, int M, int y0,
+                                          int lane, Src in, Dst out, Waiter &W, int &corner,
+                                          SwBest &tb) {
+  constexpr int R = 4;
+  const Rec16<KIND> rec(sc);
+  const int yl = y0 + lane * R + 1;  // first row of this lane
+  const int4 bq = ldg4(b_sym + (yl - 1));
+  const unsigned bp[2] = {((unsigned)bq.x & 0xffffu) | ((unsigned)bq.z << 16),
+                          ((unsigned)bq.y & 0xffffu) | ((unsigned)bq.w << 16)};
+  // P0 holds rows 0 and 2, P1 rows 1 and 3; a padding row (beyond n2) copies the row above
+  unsigned pm[2] = {0u, 0u};
+  if (yl + 0 > M) pm[0] |= 0x0000ffffu;
+  if (yl + 2 > M) pm[0] |= 0xffff0000u;
+  if (yl + 1 > M) pm[1] |= 0x0000ffffu;
+  if (yl + 3 > M) pm[1] |= 0xffff0000u;
+  const bool padwarp = __any_sync(FULL, (pm[0] | pm[1]) != 0);
+  unsigned cur[2] = {0u, 0u}, prv[2] = {0u, 0u};  // left border: stored value 0 for every kind
+  unsigned smax[2] = {0u, 0u}, sstep[2] = {0u, 0u};
+  const unsigned nn = (unsigned)N;
+
+  const int *sym = a_sym + (PADL - 1 - lane * R);
+  int win[2 * CB];
+#pragma unroll
+  for (int k = 0; k < CB; k += 4) {
+    const int4 q = ldg4(sym + k);
+    win[k] = q.x; win[k + 1] = q.y; win[k + 2] = q.z; win[k + 3] = q.w;
+  }
+  {
+    const int4 q = ldg4(sym - R);
+    win[2 * CB - R] = q.x; win[2 * CB - R + 1] = q.y; win[2 * CB - R + 2] = q.z; win[2 * CB - R + 3] = q.w;
+  }
+#pragma unroll
+  for (int k = CB; k < 2 * CB - R; ++k) win[k] = 0;
+  // the symbol pair of rows 0 and 2 at step -1 (symbol indices -1 and -3)
+  unsigned pk_prev = __byte_perm((unsigned)win[2 * CB - 1], (unsigned)win[2 * CB - 3], 0x5410);
+
+  const int row_end = ((N + 1 + CB - 1) / CB) * CB;  // ring positions carrying this row
+  unsigned recv = 0u, recv_prev = 0u;
+  int ib[2][CB];
+  bool ok_next = src_fetch<KIND>(in, 0, ib[0]);
+
+  auto chunk = [&](int j, auto checked, auto padrows) -> bool {
+    constexpr bool CK = decltype(checked)::value, PD = decltype(padrows)::value;
+    const int s0 = CB * j;
+    __syncwarp();
+    if (s0 <= N && !__all_sync(FULL, ok_next)) {
+      if (!W.wait([&] { return __all_sync(FULL, src_fetch<KIND>(in, j, ib[0])); })) return false;
+    }
+    if (in.mode == IN_RING && lane == 31) sts_vol(in.cons, in.base + min(s0 + CB, row_end));
+    if (lane == 0) recv = (unsigned)ib[0][0] << 16;
+    ok_next = src_fetch<KIND>(in, j + 1, ib[1]);
+    unsigned outq[CB];
+    const unsigned x0 = (unsigned)(s0 - lane * R - 1);  // x-1 of row 0's cell at step s0
+    const unsigned xm1[2] = {x0, x0};
+    steps_chunk16<KIND, 0, CK, PD, CB>(rec, cur, prv, recv, recv_prev, pk_prev, win, sym + s0 + CB, bp,
+                                       ib[0], outq, s0, lane, nn, xm1, pm, smax, sstep);
+    int tail[R - 1];
+#pragma unroll
+    for (int d = 0; d < R - 1; ++d) tail[d] = win[CB - R + 1 + d];
+#pragma unroll
+    for (int k = 0; k < CB; ++k) win[k] = win[k + CB];
+#pragma unroll
+    for (int d = 0; d < R - 1; ++d) win[2 * CB - R + 1 + d] = tail[d];
+#pragma unroll
+    for (int k = 0; k < CB; ++k) ib[0][k] = ib[1][k];
+    const int pos = s0 - 32 * R;
+    if (pos >= 0) {
+      int oq[CB];  // lane 31's row 3: the band's bottom row, as int32
+#pragma unroll
+      for (int k = 0; k < CB; ++k) oq[k] = (int)outq[k] >> 16;
+      if (!dst_put(out, pos, oq, lane, W)) return false;
+    }
+    return true;
+  };
+
+  using T = std::true_type;
+  using F = std::false_type;
+  const int j_end = (N + 32 * R) / CB;
+  const int j_lo = padwarp ? j_end + 1 : min((32 * R) / CB, j_end + 1);
+  const int j_hi = padwarp ? j_end : max(min((N - CB + 1) / CB, j_end), j_lo - 1);
+  for (int j = 0; j <= j_end; ++j) {
+    if (j >= j_lo && j <= j_hi) {
+      if (!chunk(j, F{}, F{})) return false;
+    } else {
+      if (!chunk(j, T{}, T{})) return false;
+    }
+  }
+  corner = (int)cur[1] >> 16;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const long long y = yl + r;
+    const int k = r & 1, sh = 16 * (r >> 1);
+    const int mx = (int)(short)(smax[k] >> sh);
+    if (KIND == K_SW && y <= M && mx > 0) {
+      const int st = (int)((sstep[k] >> sh) & 0xffffu);
+      SwBest c = {mx, 0, y, (long long)(st - lane * R - r)};
+      if (better(c, tb)) tb = c;
+    }
+  }
+  return true;
+}
+
+// A band of a job on the engine the job qualifies for.
+template <int KIND, int R>
+__device__ __forceinline__ bool sweep_job_band(bool p16, const Scoring sc, const int *a_sym, const int *b_sym,
+                                               int N, int M, int y0, int lane, Src in, Dst out, Waiter &W,
+                                               int &corner, SwBest &tb) {
+  if (R == 4 && p16) return sweep_band16<KIND>(sc, a_sym, b_sym, N, M, y0, lane, in, out, W, corner, tb);
+  return sweep_band<KIND, R>(sc, a_sym, b_sym, N, M, y0, lane, in, out, W, corner, tb);
+}
+
+// Whether a job runs on the 16-bit engine: the batch asks for it, the job's values
+// fit and the staging kernel found all of its symbols in [0, 32767].
+__device__ __forceinline__ bool job_p16(const BatchParams &P, const BatchJob &jb) {
+  return P.packed16 && fits16(jb.kind, jb.n1, jb.n2, P.sc) && P.symbad[jb.seg] == 0 &&
+         P.symbad[jb.seg + 1] == 0;
+}
+
 __device__ __forceinline__ SwBest warp_best(SwBest b) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -357,6 +484,7 @@ __device__ void block_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob
   const int *b_sym = P.sym + jb.b_off;
   const int nb = (M + 32 * R - 1) / (32 * R);
   const int L = ((N + 1 + CB - 1) / CB) * CB + 2 * CB;  // stream positions per band row
+  const bool p16 = R == 4 && job_p16(P, jb);
   SwBest tb = {0, 0, 0, 0};
   int corner = 0, corner_band = -1;
   bool ok = true;
@@ -385,7 +513,7 @@ __device__ void block_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob
       out.cons = &S.cons[warp + 1]; out.base = i * L;
     }
     int c = 0;
-    ok = sweep_band<KIND, R>(P.sc, a_sym, b_sym, N, M, band * 32 * R, lane, in, out, W, c, tb);
+    ok = sweep_job_band<KIND, R>(p16, P.sc, a_sym, b_sym, N, M, band * 32 * R, lane, in, out, W, c, tb);
     if (band == nb - 1) { corner = c; corner_band = band; }
   }
   // results: the corner from the warp that swept the last band, SW best over the CTA
@@ -447,6 +575,7 @@ __device__ void warp_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob 
   const int *b_sym = P.sym + jb.b_off;
   const int nb = (M + 32 * R - 1) / (32 * R);
   int *row = P.rows + ((long long)blockIdx.x * NW + warp) * P.stride;
+  const bool p16 = R == 4 && job_p16(P, jb);
   SwBest tb = {0, 0, 0, 0};
   int corner = 0;
   for (int band = 0; band < nb; ++band) {
@@ -458,7 +587,7 @@ __device__ void warp_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob 
     out.cons_seen = 0;
     out.mode = band == nb - 1 ? OUT_NONE : OUT_OWN;
     out.buf = row;
-    if (!sweep_band<KIND, R>(P.sc, a_sym, b_sym, N, M, band * 32 * R, lane, in, out, W, corner, tb))
+    if (!sweep_job_band<KIND, R>(p16, P.sc, a_sym, b_sym, N, M, band * 32 * R, lane, in, out, W, corner, tb))
       return;
   }
   if (KIND == K_SW) tb = warp_best(tb);
@@ -479,7 +608,7 @@ __device__ void warp_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob 
 }
 
 template <int R, int NW>
-__global__ void __launch_bounds__(NW * 32) batch_kernel(BatchParams P) {
+__global__ void __launch_bounds__(NW * 32, NW == 4 ? 3 : 1) batch_kernel(BatchParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   BatchSmem<NW> &S = *reinterpret_cast<BatchSmem<NW> *>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -562,18 +691,28 @@ __global__ void __launch_bounds__(NW * 32) batch_kernel(BatchParams P) {
   }
 }
 
-// Copies every pair's sequences into the padded, aligned layout the engine reads.
+// Copies every pair's sequences into the padded, aligned layout the engine reads,
+// and records per segment whether a symbol lies outside [0, 32767] (then the pair
+// cannot take the 16-bit engine, which compares symbols in 16-bit lanes).
 __global__ void batch_stage_kernel(const int *__restrict__ src, const long long *__restrict__ from,
                                    const long long *__restrict__ to, const int *__restrict__ len,
                                    const int *__restrict__ padl, const int *__restrict__ total,
-                                   int nseg, int *__restrict__ dst) {
+                                   int nseg, int *__restrict__ dst, int *__restrict__ bad) {
   for (int s = blockIdx.x; s < nseg; s += gridDim.x) {
     const long long f = from[s], t0 = to[s];
     const int n = len[s], pl = padl[s], tot = total[s];
+    int b = 0;
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
       const int k = i - pl;
-      dst[t0 + i] = (k >= 0 && k < n) ? src[f + k] : 0;
+      int v = 0;
+      if (k >= 0 && k < n) {
+        v = src[f + k];
+        b |= (unsigned)v > 0x7fffu;
+      }
+      dst[t0 + i] = v;
     }
+    b = __syncthreads_or(b);
+    if (threadIdx.x == 0) bad[s] = b;
   }
 }
 
@@ -725,6 +864,7 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
   auto add = [&](int i, int rows_mult, size_t slot) {
     const gme_pair &p = pairs[i];
     BatchJob j;
+    j.seg = (int)seg;
     j.a_off = place(p.a_off, p.n1, PADL, PADL + p.n1 + PADR);
     const int brows = (p.n2 + rows_mult - 1) / rows_mult * rows_mult;
     j.b_off = place(p.b_off, p.n2, 0, brows);
@@ -781,6 +921,7 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
   }
   ar.NW = NW;
   ar.grid = grid0;
+  ar.packed16 = tune.packed16 ? 1 : 0;
   ar.last_block_jobs = ar.n_b;
   ar.last_warp_jobs = ar.n_w;
   ar.last_long_jobs = (long long)ar.longj.size();
@@ -802,7 +943,7 @@ int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring 
     return ws.fail(e, "cudaMemsetAsync(batch teams)");
   const int blocks = (int)std::min<long long>(ar.nseg, 65535);
   batch_stage_kernel<<<blocks, 256, 0, st>>>(d_sym, ar.d_from, ar.d_to, ar.d_len, ar.d_padl,
-                                             ar.d_total, (int)ar.nseg, ar.d_staged);
+                                             ar.d_total, (int)ar.nseg, ar.d_staged, ar.d_symbad);
   if ((e = cudaGetLastError()) != cudaSuccess) return ws.fail(e, "batch_stage_kernel");
   BatchParams P;
   P.sym = ar.d_staged;
@@ -817,6 +958,8 @@ int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring 
   P.twrap = reinterpret_cast<unsigned long long *>(ar.d_team + (long long)ar.n_t * sizeof(TeamSlot));
   P.results = d_results;
   P.done = ar.d_done;
+  P.symbad = ar.d_symbad;
+  P.packed16 = ar.packed16;
   P.rows = ar.d_rows;
   P.wrap = ar.d_wrap;
   P.gen = ar.d_gen;

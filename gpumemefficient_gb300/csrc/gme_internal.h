@@ -45,6 +45,7 @@ struct BatchJob {
   int n1, n2;
   int kind;
   int index;  // result slot
+  int seg;    // staged segment of a (b is seg + 1): its symbols' range check
 };
 
 struct BatchTuning {
@@ -57,6 +58,8 @@ struct BatchTuning {
   long long long_min_cells = 0;
   // pairs at least this large (with 4+ band groups) run on a team of CTAs; < 0 = never
   long long team_min_cells = 1ll << 25;
+  // pairs whose values fit 16 bits run on the packed 16-bit engine
+  bool packed16 = true;
   // false: the plan takes warps, CTAs per SM and cut-offs from the tuned table
   // (gme_tuned.h) for the batch's length bucket
   bool user_set = false;
@@ -70,6 +73,8 @@ struct BatchArena {
   int *d_staged = nullptr; long long staged_cap = 0;
   long long *d_from = nullptr, *d_to = nullptr;
   int *d_len = nullptr, *d_padl = nullptr, *d_total = nullptr; long long seg_cap = 0;
+  int *d_symbad = nullptr;  // per segment: 1 if a symbol lies outside [0, 32767] (written by staging)
+  int packed16 = 0;         // the plan's choice of engine for jobs that fit 16 bits
   BatchJob *d_jobs = nullptr; long long jobs_cap = 0;
   int *d_ctrl = nullptr;
   int *d_rows = nullptr; long long rows_cap = 0;  // warp jobs' rows

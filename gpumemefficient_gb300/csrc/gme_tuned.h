@@ -15,12 +15,12 @@ struct TunedBucket {
 
 constexpr int TUNED_BUCKETS = 6;
 constexpr TunedBucket TUNED[TUNED_BUCKETS > 0 ? TUNED_BUCKETS : 1] = {
-    {32, 512, 4, 0, 4194304ll, 16777216ll},  // short: 742 GCUPS
-    {512, 2048, 4, 0, 2097152ll, 16777216ll},  // mid: 1611 GCUPS
-    {2048, 8192, 8, 0, 2097152ll, 33554432ll},  // long: 1200 GCUPS
-    {8192, 16384, 4, 2, 8388608ll, 16777216ll},  // wide: 1136 GCUPS
-    {64, 4096, 4, 0, 4194304ll, 16777216ll},  // mixed_64_4096: 1390 GCUPS
-    {32, 16384, 4, 0, 2097152ll, 16777216ll},  // mixed_32_16384: 1079 GCUPS
+    {32, 512, 4, 0, 1048576ll, 33554432ll},  // short: 785 GCUPS
+    {512, 2048, 4, 0, 2097152ll, 16777216ll},  // mid: 1710 GCUPS
+    {2048, 8192, 4, 0, 2097152ll, 16777216ll},  // long: 1250 GCUPS
+    {8192, 16384, 4, 2, 8388608ll, 16777216ll},  // wide: 1119 GCUPS
+    {64, 4096, 4, 0, 2097152ll, 33554432ll},  // mixed_64_4096: 1501 GCUPS
+    {32, 16384, 4, 0, 2097152ll, 16777216ll},  // mixed_32_16384: 1098 GCUPS
 };
 
 }  // namespace gme

@@ -143,6 +143,10 @@ typedef struct gme_batch_config {
                             * on than an even share of the batch; -1 = never) */
   int64_t team_min_cells;  /* pairs with n1*n2 >= this (and 4+ groups of bands) run on a
                             * team of CTAs (0 = 2^25; -1 = never) */
+  int32_t packed16;        /* 0 or 1: pairs whose scores provably fit 16 bits (and whose
+                            * symbols lie in [0, 32767]) run two cells per register on s16x2
+                            * DPX (the default); -1: int32 for every pair */
+  int32_t reserved;
 } gme_batch_config;
 
 gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg);

@@ -21,8 +21,8 @@ def check_batch(ctx, kinds, sa, sb, rule=0, sc=None):
     return res
 
 
-@pytest.mark.parametrize("nw", [4, 8])
-def test_mixed_uneven(gme_ctx, nw):
+@pytest.mark.parametrize("nw,packed16", [(4, -1), (8, -1), (4, 1), (8, 1)])
+def test_mixed_uneven(gme_ctx, nw, packed16):
     rng = np.random.default_rng(31 + nw)
     n = 600
     kinds = rng.integers(0, 3, n)
@@ -30,7 +30,7 @@ def test_mixed_uneven(gme_ctx, nw):
     lb = np.exp(rng.uniform(np.log(1), np.log(3000), n)).astype(int)
     sa = [rng.integers(0, 4, k) for k in la]
     sb = [rng.integers(0, 4, k) for k in lb]
-    gme_ctx.set_batch_config(warps_per_block=nw, block_min_cells=1 << 18)
+    gme_ctx.set_batch_config(warps_per_block=nw, block_min_cells=1 << 18, packed16=packed16)
     try:
         check_batch(gme_ctx, kinds, sa, sb, rule=0)
         check_batch(gme_ctx, kinds, sa, sb, rule=1)
@@ -104,13 +104,53 @@ def test_team_jobs(gme_ctx, nw):
         sa.append(rng.integers(0, 4, int(rng.integers(1, 3000))))
         sb.append(rng.integers(0, 4, int(rng.integers(1, 3000))))
     gme_ctx.set_batch_config(warps_per_block=nw, team_min_cells=1 << 18, long_min_cells=-1,
-                             block_min_cells=1 << 20)
+                             block_min_cells=1 << 20, packed16=1 if nw == 4 else -1)
     try:
         for _ in range(2):
             check_batch(gme_ctx, kinds, sa, sb, rule=1)
         st = gme_ctx.batch_stats()
         assert st["team_jobs"] > 20 and st["block_jobs"] > 0 and st["warp_jobs"] > 0
         assert st["long_jobs"] == 0
+    finally:
+        gme_ctx.set_batch_config()
+
+
+@pytest.mark.parametrize("packed16", [-1, 1])
+def test_engine_selection(gme_ctx, packed16):
+    """Pairs on the packed 16-bit engine beside pairs that must stay on int32: symbols
+    outside [0, 65535], and SW scorings whose maxima could leave 16 bits."""
+    import gpumemefficient_gb300 as g
+    rng = np.random.default_rng(404)
+    kinds, sa, sb = [], [], []
+    for i in range(90):
+        n1, n2 = int(rng.integers(1, 2500)), int(rng.integers(1, 2500))
+        if i % 3 == 0:    # full int32 range in one sequence: int32 engine
+            a = rng.integers(-2**31, 2**31 - 1, n1)
+            b = a[:n2].copy() if n2 <= n1 else rng.integers(-2**31, 2**31 - 1, n2)
+        elif i % 3 == 1:  # just above the 16-bit engine's symbol range
+            a = rng.integers(32760, 32775, n1)
+            b = rng.integers(32760, 32775, n2)
+        else:             # small alphabet: packed engine
+            a = rng.integers(0, 4, n1)
+            b = rng.integers(0, 4, n2)
+        kinds.append(i % 3 if i < 60 else 2)
+        sa.append(a)
+        sb.append(b)
+    gme_ctx.set_batch_config(packed16=packed16, block_min_cells=1 << 21)
+    try:
+        for rule in (0, 1):
+            check_batch(gme_ctx, kinds, sa, sb, rule=rule)
+        # SW maxima near and beyond the 16-bit bound (match 40: 40 x 800 = 32000)
+        sk = [2] * 12
+        sa2 = [np.zeros(n, int) for n in (700, 790, 801, 900, 2000, 3000)] * 2
+        sb2 = [np.zeros(n, int) for n in (700, 790, 801, 900, 2000, 3000)] * 2
+        check_batch(gme_ctx, sk, sa2, sb2, sc=g.scoring(40, -40, -40))
+        check_batch(gme_ctx, sk, sa2, sb2, sc=g.scoring(3, -3, -2))
+        # ED and LCS at the 16-bit bound (n1 + n2 = 32000 and just above), as block jobs
+        kinds3 = [1, 1, 0, 0]
+        sa3 = [rng.integers(0, 4, 16000), rng.integers(0, 4, 16001), rng.integers(0, 4, 16000), np.zeros(9000, int)]
+        sb3 = [rng.integers(0, 4, 16000), rng.integers(0, 4, 16000), rng.integers(0, 4, 500), np.zeros(8000, int)]
+        check_batch(gme_ctx, kinds3, sa3, sb3, rule=1)
     finally:
         gme_ctx.set_batch_config()
 
