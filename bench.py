@@ -718,7 +718,7 @@ def also_batched_served(args):
                       "parity_vs_oracle": c["parity_vs_oracle"], "roofline_frac": b["roofline"]["frac"],
                       "gpu_launches": b["gpu_launches"], "clocks": b["clocks"]}
     a = copy.copy(args)
-    a.steps, a.warmup, a.no_cpu, a.requests, a.waves, a.wave_cells = 3, 3, True, 8192, 0, 0
+    a.steps, a.warmup, a.no_cpu, a.requests, a.waves, a.wave_cells = 5, 3, True, 8192, 0, 0
     a.rates, a.rate_seconds, a.no_parity = [0.1, 0.5, 0.8], 1.5, False
     s = run_gme_served(a)
     c = s["config"]
