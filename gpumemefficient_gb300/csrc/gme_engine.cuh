@@ -66,6 +66,27 @@ __device__ __forceinline__ unsigned long long entry(int pos, int v) {
 }
 
 __device__ __forceinline__ int4 ldg4(const int *p) { return __ldg(reinterpret_cast<const int4 *>(p)); }
+__device__ __forceinline__ int2 ldg2(const int *p) { return __ldg(reinterpret_cast<const int2 *>(p)); }
+
+// n consecutive symbols from p into d[0..n): 16-byte loads when the lane's symbol base
+// is 16-byte aligned (R a multiple of 4), else 8-byte loads (R = 2).
+template <int R, int n>
+__device__ __forceinline__ void ld_syms(const int *p, int *d) {
+  if constexpr (R % 4 == 0) {
+#pragma unroll
+    for (int k = 0; k < n; k += 4) {
+      const int4 q = ldg4(p + k);
+      d[k] = q.x; d[k + 1] = q.y; d[k + 2] = q.z; d[k + 3] = q.w;
+    }
+  } else {
+    static_assert(R % 2 == 0 && n % 2 == 0, "8-byte symbol loads need even R and n");
+#pragma unroll
+    for (int k = 0; k < n; k += 2) {
+      const int2 q = ldg2(p + k);
+      d[k] = q.x; d[k + 1] = q.y;
+    }
+  }
+}
 
 // ---------------------------------------------------------------------------
 // C wavefront steps of one lane (R rows): one ring transaction per C steps.
@@ -96,14 +117,7 @@ __device__ __forceinline__ void steps_chunk(const Rec<KIND> &rec, int (&cur)[R],
   static_assert(R < CH, "the window refill at step R needs R < CH");
 #pragma unroll
   for (int q = 0; q < CH; ++q) {
-    if (q == R) {
-#pragma unroll
-      for (int i = 0; i < CH / 4; ++i) {
-        const int4 v = ldg4(sym_next + 4 * i);
-        const int h = (PAR ^ 1) * CH + 4 * i;
-        win[h] = v.x; win[h + 1] = v.y; win[h + 2] = v.z; win[h + 3] = v.w;
-      }
-    }
+    if (q == R) ld_syms<R, CH>(sym_next, &win[(PAR ^ 1) * CH]);
     const int s = s0 + q;
     const int rcv = recv;  // the cell above row 0 for this step
     outq[q] = cur[R - 1];  // lane 31: bottom cell after step s-1 (column s-32R)

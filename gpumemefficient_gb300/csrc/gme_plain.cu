@@ -31,6 +31,7 @@
 //     between global memory and the first/last rings.
 //   * Nothing of the table is kept: memory is O(n1) per band in flight, the
 //     last row/column are produced on the fly.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
@@ -38,6 +39,7 @@
 
 #include "gme_engine.cuh"
 #include "gme_internal.h"
+#include "gme_tuned_plain.h"
 
 namespace gme {
 
@@ -81,11 +83,7 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
   const int N = P.N, M = P.M;
   const int yl = band * P.H + warp * 32 * R + lane * R + 1;  // first row of this lane
   int bs[R], cur[R], prv[R], smax[R], sstep[R];
-#pragma unroll
-  for (int r = 0; r < R; r += 4) {
-    int4 q = ldg4(P.b_pad + (yl - 1 + r));
-    bs[r] = q.x; bs[r + 1] = q.y; bs[r + 2] = q.z; bs[r + 3] = q.w;
-  }
+  ld_syms<R, R>(P.b_pad + (yl - 1), bs);
   unsigned padmask = 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
@@ -100,17 +98,8 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
   // Symbol window for chunk 0: i in [0, C) at win[0..C), i in [-R, 0) at win[2C-R..2C).
   const int *sym = P.a_pad + (PADL - 1 - lane * R);  // sym[i]: symbol index i of this lane
   int win[2 * C];
-#pragma unroll
-  for (int k = 0; k < C; k += 4) {
-    const int4 q = ldg4(sym + k);
-    win[k] = q.x; win[k + 1] = q.y; win[k + 2] = q.z; win[k + 3] = q.w;
-  }
-#pragma unroll
-  for (int k = 0; k < R; k += 4) {
-    const int4 q = ldg4(sym - R + k);
-    win[2 * C - R + k] = q.x; win[2 * C - R + k + 1] = q.y;
-    win[2 * C - R + k + 2] = q.z; win[2 * C - R + k + 3] = q.w;
-  }
+  ld_syms<R, C>(sym, win);
+  ld_syms<R, R>(sym - R, &win[2 * C - R]);
 #pragma unroll
   for (int k = C; k < 2 * C - R; ++k) win[k] = 0;
 
@@ -471,6 +460,12 @@ static cudaError_t launch_plain_t(const PlainParams &P, int grid, cudaStream_t s
 
 template <int KIND>
 static cudaError_t launch_plain_k(int R, int NW, const PlainParams &P, int grid, cudaStream_t st) {
+  if (R == 2) {
+    switch (NW) {
+      case 4: return launch_plain_t<KIND, 2, 4>(P, grid, st);
+      case 8: return launch_plain_t<KIND, 2, 8>(P, grid, st);
+    }
+  }
   if (R == 4) {
     switch (NW) {
       case 1: return launch_plain_t<KIND, 4, 1>(P, grid, st);
@@ -485,19 +480,31 @@ static cudaError_t launch_plain_k(int R, int NW, const PlainParams &P, int grid,
 }
 
 bool plain_config_valid(int R, int NW) {
-  return R == 4 && (NW == 1 || NW == 2 || NW == 3 || NW == 4 || NW == 6 || NW == 8);
+  return (R == 4 && (NW == 1 || NW == 2 || NW == 3 || NW == 4 || NW == 6 || NW == 8)) ||
+         (R == 2 && (NW == 4 || NW == 8));
 }
 
 // Automatic shape.  Every band boundary costs one L2 hand-off on the critical
 // path and a band that has to wait for a free CTA doubles the sweep, so take the
 // shortest band (most SMs busy) for which all bands run at once, one per SM.
+// Rows per lane and warps per band: the tuned table's entry for the nearest table
+// height (gme_tuned_plain.h, swept by gpumemefficient_gb300/tune.py), else the
+// smallest band that keeps every band on its own SM.
 void plain_auto_config(int sms, long long n1, long long n2, int *R, int *NW, int *grid) {
   (void)n1;
   static const int cand[][2] = {{4, 1}, {4, 2}, {4, 3}, {4, 4}, {4, 6}, {4, 8}};
   int r = 4, nw = 8;
-  for (const auto &c : cand) {
-    const long long H = (long long)c[1] * 32 * c[0];
-    if ((n2 + H - 1) / H <= sms) { r = c[0]; nw = c[1]; break; }
+  if (TUNED_PLAIN > 0) {
+    double best = 1e30;
+    for (int k = 0; k < TUNED_PLAIN; ++k) {
+      const double d = std::fabs(std::log((double)std::max<long long>(n2, 1) / TUNED_PLAIN_TABLE[k].n));
+      if (d < best) { best = d; r = TUNED_PLAIN_TABLE[k].rows_per_lane; nw = TUNED_PLAIN_TABLE[k].warps_per_band; }
+    }
+  } else {
+    for (const auto &c : cand) {
+      const long long H = (long long)c[1] * 32 * c[0];
+      if ((n2 + H - 1) / H <= sms) { r = c[0]; nw = c[1]; break; }
+    }
   }
   *R = r;
   *NW = nw;

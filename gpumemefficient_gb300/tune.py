@@ -201,6 +201,92 @@ def header_from_json(path=TUNED_JSON):
     gen_header(json.load(open(path))["best"])
 
 
+# ---- the plain path: one pair per call --------------------------------------------
+PLAIN_SIZES = [2048, 4096, 8192, 16384, 32768, 65536]
+PLAIN_SHAPES = [(4, 1), (4, 2), (4, 4), (4, 8), (2, 4), (2, 8)]
+TUNED_PLAIN_H = os.path.join(HERE, "csrc", "gme_tuned_plain.h")
+
+
+def sweep_plain(sizes=None, shapes=None, reps: int = 5, device: int = 0, log=print):
+    """Per square size n (edit distance, n x n, seeded): rows per lane x warps per band,
+    with the grid at one CTA per band up to the SM count (0) and, for more bands than
+    SMs, the SM count; times one call by CUDA events.  Results must equal the first
+    shape's."""
+    import torch
+    from . import Context
+    sizes = sizes or PLAIN_SIZES
+    shapes = shapes or PLAIN_SHAPES
+    ctx = Context(device)
+    dev = torch.device("cuda", device)
+    st = torch.cuda.Stream(device=device)
+    out = torch.zeros(32, dtype=torch.uint8, device=dev)
+    rows = []
+    for n in sizes:
+        rng = np.random.default_rng(0xF00D + n)
+        a = torch.from_numpy(rng.integers(0, 4, n).astype(np.int32)).to(dev)
+        b = torch.from_numpy(rng.integers(0, 4, n).astype(np.int32)).to(dev)
+        ref = None
+        for R, NW in shapes:
+            ctx.set_plain_config(R, NW, 0)
+            for _ in range(2):
+                ctx.align_device(1, a.data_ptr(), n, b.data_ptr(), n, out.data_ptr(), stream=st.cuda_stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(reps):
+                ctx.align_device(1, a.data_ptr(), n, b.data_ptr(), n, out.data_ptr(), stream=st.cuda_stream)
+            e1.record(st)
+            st.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            score = bytes(out.cpu().numpy())[:4]
+            if ref is None:
+                ref = score
+            row = {"n": n, "rows_per_lane": R, "warps_per_band": NW, "grid": ctx.plain_config(n, n)["grid"],
+                   "ms": ms, "gcups": n * n / ms / 1e6, "ok": score == ref}
+            rows.append(row)
+            log(json.dumps(row))
+    ctx.set_plain_config()
+    ctx.close()
+    return rows
+
+
+def gen_plain_header(rows, path=TUNED_PLAIN_H):
+    """Best shape per size as the table plain_auto_config reads (nearest size wins)."""
+    best = {}
+    for r in rows:
+        if r["ok"] and (r["n"] not in best or r["gcups"] > best[r["n"]]["gcups"]):
+            best[r["n"]] = r
+    out = ["// gme_tuned_plain.h -- plain-path shape per table height, written by",
+           "// gpumemefficient_gb300/tune.py (sweep_plain) from a sweep on GB300: edit distance",
+           "// on square pairs.  plain_auto_config takes the entry whose n is nearest (in log",
+           "// scale) to the pair's row count n2.",
+           "#pragma once", "", "namespace gme {", "",
+           "struct TunedPlain {", "  int n, rows_per_lane, warps_per_band;", "};", "",
+           f"constexpr int TUNED_PLAIN = {len(best)};",
+           "constexpr TunedPlain TUNED_PLAIN_TABLE[TUNED_PLAIN > 0 ? TUNED_PLAIN : 1] = {"]
+    for n in sorted(best):
+        r = best[n]
+        out.append(f"    {{{n}, {r['rows_per_lane']}, {r['warps_per_band']}}},  // {r['gcups']:.0f} GCUPS")
+    if not best:
+        out.append("    {0, 4, 4},")
+    out += ["};", "", "}  // namespace gme", ""]
+    with open(path, "w") as f:
+        f.write("\n".join(out))
+    return best
+
+
+def write_plain_md(rows, best, path, cmd):
+    lines = ["# Plain-path autotune sweep (edit distance, n x n)", "", f"Command (GB300): `{cmd}`", "",
+             "One call per shape, CUDA-event time, mean of the repetitions; grid = one CTA per band "
+             "up to the SM count.  Every shape's score equals the first shape's.", "",
+             "| n | rows/lane | warps/band | grid | ms | GCUPS | |", "|---:|---:|---:|---:|---:|---:|---|"]
+    for r in rows:
+        mark = "best" if best.get(r["n"]) is r else ("" if r["ok"] else "MISMATCH")
+        lines.append(f"| {r['n']} | {r['rows_per_lane']} | {r['warps_per_band']} | {r['grid']} | "
+                     f"{r['ms']:.3f} | {r['gcups']:.1f} | {mark} |")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--out-json", default=TUNED_JSON)
@@ -209,8 +295,24 @@ def main():
     p.add_argument("--cells", type=float, default=1.5e10)
     p.add_argument("--reps", type=int, default=5)
     p.add_argument("--header", action="store_true", help="also regenerate csrc/gme_tuned.h")
+    p.add_argument("--plain", action="store_true",
+                   help="sweep the plain path instead (writes csrc/gme_tuned_plain.h with --header)")
     a = p.parse_args()
     t0 = time.time()
+    if a.plain:
+        rows = sweep_plain()
+        best = gen_plain_header(rows) if a.header else {}
+        if a.out_md:
+            if not best:
+                best = {}
+                for r in rows:
+                    if r["ok"] and (r["n"] not in best or r["gcups"] > best[r["n"]]["gcups"]):
+                        best[r["n"]] = r
+            write_plain_md(rows, best, a.out_md, "python -m gpumemefficient_gb300.tune --plain --header "
+                           f"--out-md {a.out_md}")
+        with open(a.out_json, "w") as f:
+            json.dump({"plain_rows": rows, "seconds": time.time() - t0}, f, indent=1)
+        return
     rows = sweep(QUICK_GRID if a.quick else GRID, a.cells, a.reps)
     best = winners(rows)
     with open(a.out_json, "w") as f:

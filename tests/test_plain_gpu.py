@@ -7,7 +7,7 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-CONFIGS = [(4, 1), (4, 2), (4, 3), (4, 4), (4, 6), (4, 8)]
+CONFIGS = [(4, 1), (4, 2), (4, 3), (4, 4), (4, 6), (4, 8), (2, 4), (2, 8)]
 
 
 def check(ctx, kind, a, b, rule=0, sc=None):
