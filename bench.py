@@ -268,12 +268,9 @@ def run_gme(args):
     launches = ctx.launches - launches0
     clk = clocks.stop()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    t_dev = sum(step_ms) / 1e3
-    if ws > 1:
-        t = torch.tensor([t_dev], dtype=torch.float64, device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
-    value = ws * cells * args.steps / t_dev / 1e9
+    from gpumemefficient_gb300.replicas import aggregate
+    t_dev, job_cells = aggregate(sum(step_ms) / 1e3, cells * args.steps, device=f"cuda:{local}")
+    value = job_cells / t_dev / 1e9
 
     # end to end through the C ABI with pinned host buffers
     ha = torch.from_numpy(a).pin_memory().numpy()
@@ -286,12 +283,8 @@ def run_gme(args):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         r = ctx.align(kind, ha, hb, sc=sc)
-    t_e2e = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([t_e2e], dtype=torch.float64, device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(t.item())
-    e2e = {"value": ws * cells * e2e_steps / t_e2e / 1e9, "unit": "GCUPS",
+    t_e2e, e2e_cells = aggregate(time.perf_counter() - t0, cells * e2e_steps, device=f"cuda:{local}")
+    e2e = {"value": e2e_cells / t_e2e / 1e9, "unit": "GCUPS",
            "h2d_bytes_per_step": int(a.nbytes + b.nbytes), "d2h_bytes_per_step": 32,
            "steps": e2e_steps, "score_ok": r.score == o["score"]}
 
@@ -394,12 +387,9 @@ def run_gme_batch(args):
     launches = ctx.launches - launches0
     clk = clocks.stop()
     step_ms = [s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)]
-    t_dev = sum(step_ms) / 1e3
-    if ws > 1:
-        t = torch.tensor([t_dev], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
-    value = ws * cells * args.steps / t_dev / 1e9
+    from gpumemefficient_gb300.replicas import aggregate
+    t_dev, job_cells = aggregate(sum(step_ms) / 1e3, cells * args.steps, device=dev)
+    value = job_cells / t_dev / 1e9
     mean_s = t_dev / args.steps
 
     # end to end through the C ABI: pinned host symbols in, results out, plan made per call
