@@ -649,6 +649,59 @@ def run_gme_served(args):
     return line
 
 
+def run_gme_path(args):
+    """Alignment path of the headline pair (Hirschberg on the GPU): the same GCUPS metric
+    over the n1 x n2 cells of the problem (the traceback itself computes about twice
+    that many), host sequences in, the edit script out."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    import __graft_entry__ as ge
+    ge.build()
+    import gpumemefficient_gb300 as g
+    from oracle import oracle as O
+    kind, a, b, cfg = workload("ed65536" if args.workload == "path" else args.workload)
+    ctx = g.Context(local)
+    score, ops = ctx.align_path(kind, a, b)
+    want = O.align(kind, a, b, rule=O.ED_STANDARD, threads=os.cpu_count() or 1)["score"]
+    cost = sum(1 for c in ops if c != "M") + sum(1 for i, j, c in _walk(ops) if c == "M" and a[i] != b[j])
+    parity = score == want and cost == want
+    for _ in range(args.warmup):
+        ctx.align_path(kind, a, b)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ctx.align_path(kind, a, b)
+        times.append(time.perf_counter() - t0)
+    cells = len(a) * len(b)
+    t = sum(times) / len(times)
+    cfg = dict(cfg)
+    cfg.update({"workload": cfg["workload"] + "; optimal alignment path (edit script), Hirschberg on the GPU",
+                "ed_boundary": "standard", "parity_vs_oracle": "ok" if parity else "MISMATCH",
+                "script_length": len(ops), "score": score})
+    line = {"metric": METRIC, "value": cells / t / 1e9, "unit": "GCUPS", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded)", "config": cfg,
+            "e2e": {"value": cells / t / 1e9, "unit": "GCUPS", "h2d_bytes_per_step": int(a.nbytes + b.nbytes),
+                    "d2h_bytes_per_step": len(ops)},
+            "gpu_launches": None, "roofline": None, "cpu_baseline": None}
+    ctx.close()
+    return line
+
+
+def _walk(ops):
+    i = j = 0
+    for c in ops:
+        yield i, j, c
+        if c == "M":
+            i += 1
+            j += 1
+        elif c == "D":
+            i += 1
+        else:
+            j += 1
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -683,6 +736,8 @@ def main():
         line = run_gme_batch(args)
     elif args.workload == "served":
         line = run_gme_served(args)
+    elif args.workload == "path":
+        line = run_gme_path(args)
     else:
         line = run_gme(args)
         ws = dist_env()[0]

@@ -126,6 +126,8 @@ def _declare(L):
     L.gme_server_get_stats.argtypes = [_vp, c.POINTER(ServerStats)]
     L.gme_server_last_error.argtypes = [_vp]
     L.gme_server_last_error.restype = c.c_char_p
+    L.gme_align_path.argtypes = [_vp, c.c_int, _vp, c.c_int64, _vp, c.c_int64, c.POINTER(Scoring), _vp,
+                                 c.c_int64, c.POINTER(c.c_int64), c.POINTER(c.c_int32)]
     L.gme_debug_wait_timeout.argtypes = [_vp, c.c_uint64, c.POINTER(c.c_int32)]
     L.gme_launch_count.argtypes = [_vp]
     L.gme_launch_count.restype = c.c_int64
@@ -269,6 +271,22 @@ class Context:
         _check(lib().gme_align_batch_device(self.handle, d_symbols, nsym, pairs.ctypes.data,
                                             len(pairs), ctypes.byref(sc), d_results,
                                             stream or None), self.handle)
+
+    def align_path(self, kind, a, b):
+        """(score, edit script) of an optimal global alignment: 'M' a[i]~b[j], 'D' a[i]~gap,
+        'I' gap~b[j].  LCS, or ED with the standard border."""
+        kind = KINDS.get(kind, kind) if isinstance(kind, str) else kind
+        a = np.ascontiguousarray(a, dtype=np.int32)
+        b = np.ascontiguousarray(b, dtype=np.int32)
+        cap = len(a) + len(b)
+        buf = ctypes.create_string_buffer(max(cap, 1))
+        n = ctypes.c_int64()
+        sc_ = ctypes.c_int32()
+        scoring_ = scoring(ed_boundary=ED_STANDARD)
+        _check(lib().gme_align_path(self.handle, kind, a.ctypes.data, len(a), b.ctypes.data, len(b),
+                                    ctypes.byref(scoring_), buf, cap, ctypes.byref(n), ctypes.byref(sc_)),
+               self.handle)
+        return sc_.value, buf.raw[:n.value].decode()
 
     def debug_wait_timeout(self, timeout_ns: int) -> int:
         """Runs a bounded device wait on a flag nothing sets; returns the kernel's status."""

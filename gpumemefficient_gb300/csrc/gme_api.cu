@@ -665,6 +665,7 @@ long long ctx_device_bytes(const gme_context *ctx) {
 }
 
 int ctx_sms(const gme_context *ctx) { return ctx->ws.sms; }
+int ctx_device(const gme_context *ctx) { return ctx->device; }
 
 int ctx_batch_status(gme_context *ctx) {
   int v = 0;

@@ -140,6 +140,7 @@ cudaStream_t ctx_stream(gme_context *ctx);
 void ctx_set_served(gme_context *ctx, int *d_done);
 long long ctx_device_bytes(const gme_context *ctx);
 int ctx_sms(const gme_context *ctx);
+int ctx_device(const gme_context *ctx);
 // the status word of the context's last batch kernel (read after it has finished)
 int ctx_batch_status(gme_context *ctx);
 

@@ -246,6 +246,22 @@ gme_status gme_server_get_stats(const gme_server *s, gme_server_stats *out);
 /* Text of the last error the server met (never NULL). */
 const char *gme_server_last_error(const gme_server *s);
 
+/* ---- alignment paths -------------------------------------------------------------
+ * An optimal global alignment as an edit script, in memory linear in n1 + n2
+ * (Hirschberg: the plain kernel's exported last rows of a forward and a backward
+ * half-problem split it at the middle row; small subproblems are solved whole on
+ * the GPU).  ops[k]: 'M' aligns a[i] with b[j] (LCS: only where equal), 'D' takes
+ * a[i] against a gap, 'I' takes b[j] against a gap.  LCS maximises the number of
+ * 'M'; ED uses the standard border (row 0 = 0, 1, 2, ...; sc may be NULL or must say
+ * GME_ED_STANDARD) and minimises insertions, deletions and mismatches.  SW is not
+ * supported (GME_ERR_INVALID).  *n_ops gets the script length (at most n1 + n2) and
+ * *score the optimal score; with ops NULL only those are returned; GME_ERR_INVALID
+ * if ops_cap is too small.  No counterpart in the reference, which returns scores
+ * only (its boundary rows are what make the traceback possible). */
+gme_status gme_align_path(gme_context *ctx, gme_kind kind, const int32_t *a, int64_t n1,
+                          const int32_t *b, int64_t n2, const gme_scoring *sc, char *ops,
+                          int64_t ops_cap, int64_t *n_ops, int32_t *score);
+
 /* ---- plain path without allocation --------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc (code
  * running inside another runtime's memory pool, a plugin that must not allocate on
