@@ -110,6 +110,8 @@ def _declare(L):
     L.gme_align_batch.argtypes = [_vp, _vp, c.c_int64, _vp, c.c_int64, c.POINTER(Scoring), _vp]
     L.gme_align_batch_device.argtypes = [_vp, _vp, c.c_int64, _vp, c.c_int64, c.POINTER(Scoring),
                                          _vp, _vp]
+    L.gme_align_batch_device_rows.argtypes = [_vp, _vp, c.c_int64, _vp, c.c_int64, c.POINTER(Scoring), _vp,
+                                              _vp, _vp, _vp, _vp, _vp]
     L.gme_batch_stats.argtypes = [_vp, c.POINTER(c.c_int64), c.POINTER(c.c_int64),
                                   c.POINTER(c.c_int64), c.POINTER(c.c_int64)]
     L.gme_batch_plan_create.argtypes = [_vp, _vp, c.c_int64, c.c_int64, c.POINTER(c.c_void_p)]
@@ -262,6 +264,19 @@ class Context:
                                      pairs.ctypes.data, len(pairs), ctypes.byref(sc),
                                      res.ctypes.data), self.handle)
         return res
+
+    def align_batch_device_rows(self, d_symbols: int, nsym: int, pairs: np.ndarray, d_results: int,
+                                d_last_rows: int = 0, row_offsets=None, d_last_cols: int = 0,
+                                col_offsets=None, sc: Optional[Scoring] = None, stream: int = 0):
+        """Device batch with each pair's last row/column written at the given element offsets."""
+        pairs = np.ascontiguousarray(pairs, PAIR_DTYPE)
+        ro = np.ascontiguousarray(row_offsets, np.int64) if row_offsets is not None else None
+        co = np.ascontiguousarray(col_offsets, np.int64) if col_offsets is not None else None
+        sc = sc or scoring()
+        _check(lib().gme_align_batch_device_rows(
+            self.handle, d_symbols, nsym, pairs.ctypes.data, len(pairs), ctypes.byref(sc), d_results,
+            d_last_rows or None, ro.ctypes.data if ro is not None else None, d_last_cols or None,
+            co.ctypes.data if co is not None else None, stream or None), self.handle)
 
     def align_batch_device(self, d_symbols: int, nsym: int, pairs: np.ndarray, d_results: int,
                            sc: Optional[Scoring] = None, stream: int = 0):

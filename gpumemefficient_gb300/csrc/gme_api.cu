@@ -415,13 +415,14 @@ gme_status gme_align(gme_context *ctx, gme_kind kind, const int32_t *a, int64_t 
   return GME_OK;
 }
 
-// the plain path for the pairs a batch hands over (too wide for shared rows, or empty)
+// the plain path for the pairs a batch hands over (too wide for the batch kernel's rows,
+// empty, or very large)
 static int batch_plain_cb(void *p, int kind, const int *d_a, long long n1, const int *d_b, long long n2,
-                          gme_result *d_out) {
+                          gme_result *d_out, int *d_last_row, int *d_last_col) {
   struct Arg { gme_context *ctx; const gme_scoring *sc; cudaStream_t st; };
   Arg *a = (Arg *)p;
-  return (int)gme_align_device(a->ctx, (gme_kind)kind, d_a, n1, d_b, n2, a->sc, d_out, nullptr,
-                               nullptr, a->st);
+  return (int)gme_align_device(a->ctx, (gme_kind)kind, d_a, n1, d_b, n2, a->sc, d_out, d_last_row,
+                               d_last_col, a->st);
 }
 
 gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg) {
@@ -472,7 +473,36 @@ gme_status gme_align_batch_device(gme_context *ctx, const int32_t *d_symbols, in
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
   struct { gme_context *ctx; const gme_scoring *sc; cudaStream_t st; } arg = {ctx, sc, st};
   int rc = gme::batch_run(ctx->ws, ctx->batch, d_symbols, nsym, pairs, npairs, to_scoring(sc),
-                          d_results, st, ctx->batch_tune, ctx->timeout_ns, batch_plain_cb, &arg);
+                          d_results, st, ctx->batch_tune, ctx->timeout_ns, nullptr, nullptr, nullptr,
+                          nullptr, batch_plain_cb, &arg);
+  return to_status(rc);
+}
+
+gme_status gme_align_batch_device_rows(gme_context *ctx, const int32_t *d_symbols, int64_t nsym,
+                                       const gme_pair *pairs, int64_t npairs, const gme_scoring *sc,
+                                       gme_result *d_results, int32_t *d_last_rows,
+                                       const int64_t *row_offsets, int32_t *d_last_cols,
+                                       const int64_t *col_offsets, void *stream) {
+  if (!ctx || npairs < 0 || (npairs > 0 && (!pairs || !d_results || !d_symbols)) || nsym < 0 ||
+      (d_last_rows && !row_offsets) || (d_last_cols && !col_offsets))
+    return GME_ERR_INVALID;
+  if (npairs == 0) return GME_OK;
+  gme_scoring def = gme_default_scoring();
+  if (!sc) sc = &def;
+  for (int64_t i = 0; i < npairs; ++i) {
+    gme_status s = check_sizes(ctx, (gme_kind)pairs[i].kind, pairs[i].n1, pairs[i].n2, sc);
+    if (s != GME_OK) {
+      ctx->ws.last_error = "pair " + std::to_string(i) + ": " + ctx->ws.last_error;
+      return s;
+    }
+  }
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  struct { gme_context *ctx; const gme_scoring *sc; cudaStream_t st; } arg = {ctx, sc, st};
+  int rc = gme::batch_run(ctx->ws, ctx->batch, d_symbols, nsym, pairs, npairs, to_scoring(sc),
+                          d_results, st, ctx->batch_tune, ctx->timeout_ns, d_last_rows,
+                          (const long long *)row_offsets, d_last_cols, (const long long *)col_offsets,
+                          batch_plain_cb, &arg);
   return to_status(rc);
 }
 
@@ -609,7 +639,7 @@ gme_status gme_batch_plan_run(gme_batch_plan *p, const int32_t *d_symbols, const
     }
   }
   struct { gme_context *ctx; const gme_scoring *sc; cudaStream_t st; } arg = {ctx, sc, st};
-  return to_status(gme::batch_long(p->ar, d_symbols, d_results, batch_plain_cb, &arg));
+  return to_status(gme::batch_long(p->ar, d_symbols, d_results, nullptr, nullptr, batch_plain_cb, &arg));
 }
 
 gme_status gme_batch_plan_destroy(gme_batch_plan *p) {

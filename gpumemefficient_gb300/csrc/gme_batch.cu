@@ -63,6 +63,8 @@ struct BatchParams {
   unsigned long long *twrap;  // two tagged rows of `stride` words per team job (cleared likewise)
   gme_result *results;
   int *done;               // optional: done[index] = 1 once results[index] is written (system scope)
+  int *last_rows;          // optional: per job, its last row at jobs' row_off
+  int *last_cols;          // optional: per job, its last column at jobs' col_off
   const int *symbad;       // per staged segment: 1 if a symbol lies outside [0, 32767]
   int packed16;            // jobs that qualify take the packed 16-bit engine
   int *rows;               // warp jobs: one row of `stride` ints per warp of the grid (L2-resident)
@@ -91,7 +93,7 @@ template <int NW> struct __align__(16) BatchSmem {
 // predictable branch per chunk and one sweep routine serves every combination.
 // ---------------------------------------------------------------------------
 enum : int { IN_TOP = 0, IN_RING = 1, IN_ROW = 2, IN_OWN = 3 };
-enum : int { OUT_NONE = 0, OUT_RING = 1, OUT_ROW = 2, OUT_OWN = 3 };
+enum : int { OUT_NONE = 0, OUT_RING = 1, OUT_ROW = 2, OUT_OWN = 3, OUT_USER = 4 };
 
 struct Src {
   int mode;
@@ -106,13 +108,15 @@ struct Src {
 
 struct Dst {
   int mode;
-  int *buf;
+  int *buf;          // ring or own row; OUT_USER: the caller's last row (table values)
   int *tags;
   unsigned long long *row;
   const int *cons;
   int base;
   unsigned tag;
   int cons_seen;
+  int N, M;          // OUT_USER: columns 0..N are written, row M's values (ED adds x + y)
+  int addxy;
 };
 
 __device__ __forceinline__ void ld_vol_u64x2(const unsigned long long *p, unsigned long long &a,
@@ -171,6 +175,15 @@ __device__ __forceinline__ bool src_fetch(const Src &s, int j, int (&d)[CB]) {
 
 __device__ __forceinline__ bool dst_put(Dst &o, int pos, const int (&q)[CB], int lane, Waiter &W) {
   if (o.mode == OUT_NONE) return true;
+  if (o.mode == OUT_USER) {
+    // the pair's last row, as table values, for the caller
+    if (lane == 31) {
+#pragma unroll
+      for (int k = 0; k < CB; ++k)
+        if (pos + k <= o.N) o.buf[pos + k] = q[k] + (o.addxy ? pos + k + o.M : 0);
+    }
+    return true;
+  }
   if (o.mode == OUT_ROW) {
     if (lane == 31) {
       const unsigned long long t = (unsigned long long)o.tag << 32;
@@ -212,7 +225,7 @@ template <int KIND, int R>
 __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict__ a_sym,
                                         const int *__restrict__ b_sym, int N, int M, int y0,
                                         int lane, Src in, Dst out, Waiter &W, int &corner,
-                                        SwBest &tb) {
+                                        SwBest &tb, int *col_out) {
   const Rec<KIND> rec(sc);
   const int yl = y0 + lane * R + 1;  // first row of this lane
   int bs[R], cur[R], prv[R], smax[R], sstep[R];
@@ -307,6 +320,7 @@ __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict_
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const long long y = yl + r;
+    if (col_out && y <= M) col_out[y] = Rec<KIND>::to_v(cur[r], N, y);  // column N, for the caller
     if (KIND == K_SW && y <= M && smax[r] > 0) {
       SwBest c = {smax[r], 0, y, (long long)(sstep[r] - lane * R - r)};
       if (better(c, tb)) tb = c;
@@ -323,7 +337,7 @@ template <int KIND>
 __device__ __noinline__ bool sweep_band16(const Scoring sc, const int *__restrict__ a_sym,
                                           const int *__restrict__ b_sym, int N, int M, int y0,
                                           int lane, Src in, Dst out, Waiter &W, int &corner,
-                                          SwBest &tb) {
+                                          SwBest &tb, int *col_out) {
   constexpr int R = 4;
   const Rec16<KIND> rec(sc);
   const int yl = y0 + lane * R + 1;  // first row of this lane
@@ -413,6 +427,7 @@ __device__ __noinline__ bool sweep_band16(const Scoring sc, const int *__restric
   for (int r = 0; r < R; ++r) {
     const long long y = yl + r;
     const int k = r & 1, sh = 16 * (r >> 1);
+    if (col_out && y <= M) col_out[y] = Rec<KIND>::to_v((int)(short)(cur[k] >> sh), N, y);
     const int mx = (int)(short)(smax[k] >> sh);
     if (KIND == K_SW && y <= M && mx > 0) {
       const int st = (int)((sstep[k] >> sh) & 0xffffu);
@@ -427,9 +442,9 @@ __device__ __noinline__ bool sweep_band16(const Scoring sc, const int *__restric
 template <int KIND, int R>
 __device__ __forceinline__ bool sweep_job_band(bool p16, const Scoring sc, const int *a_sym, const int *b_sym,
                                                int N, int M, int y0, int lane, Src in, Dst out, Waiter &W,
-                                               int &corner, SwBest &tb) {
-  if (R == 4 && p16) return sweep_band16<KIND>(sc, a_sym, b_sym, N, M, y0, lane, in, out, W, corner, tb);
-  return sweep_band<KIND, R>(sc, a_sym, b_sym, N, M, y0, lane, in, out, W, corner, tb);
+                                               int &corner, SwBest &tb, int *col_out) {
+  if (R == 4 && p16) return sweep_band16<KIND>(sc, a_sym, b_sym, N, M, y0, lane, in, out, W, corner, tb, col_out);
+  return sweep_band<KIND, R>(sc, a_sym, b_sym, N, M, y0, lane, in, out, W, corner, tb, col_out);
 }
 
 // Whether a job runs on the 16-bit engine: the batch asks for it, the job's values
@@ -450,6 +465,31 @@ __device__ __forceinline__ SwBest warp_best(SwBest b) {
     if (better(c, b)) b = c;
   }
   return b;
+}
+
+// Where the band that ends a job sends its bottom row: the caller's last row if asked
+// for (row n2 as table values), else nowhere.
+template <int KIND>
+__device__ __forceinline__ void last_row_dst(const BatchParams &P, const BatchJob &jb, Dst &out) {
+  if (P.last_rows && jb.row_off >= 0) {
+    out.mode = OUT_USER;
+    out.buf = P.last_rows + jb.row_off;
+    out.N = jb.n1;
+    out.M = jb.n2;
+    out.addxy = KIND == K_ED;
+  } else {
+    out.mode = OUT_NONE;
+  }
+}
+
+// Where a band writes its rows' values at column n1 (the job's last column), or
+// null; the first band's lane 0 also writes row 0 (the top border at column n1).
+template <int KIND>
+__device__ __forceinline__ int *col_dst(const BatchParams &P, const BatchJob &jb, int band, int lane) {
+  if (!P.last_cols || jb.col_off < 0) return nullptr;
+  int *c = P.last_cols + jb.col_off;
+  if (band == 0 && lane == 0) c[0] = Rec<KIND>::to_v(Rec<KIND>::top(jb.n1, P.sc.ed_rule), jb.n1, 0);
+  return c;
 }
 
 // A job's status: a timeout if any wait of this CTA or of the launch gave up (a
@@ -505,7 +545,7 @@ __device__ void block_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob
     Dst out;
     out.cons_seen = 0;
     if (band == nb - 1) {
-      out.mode = OUT_NONE;
+      last_row_dst<KIND>(P, jb, out);
     } else if (warp == NW - 1) {
       out.mode = OUT_ROW; out.row = wrap + (g & 1) * P.stride; out.tag = tag0 + g + 1;
     } else {
@@ -513,7 +553,8 @@ __device__ void block_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob
       out.cons = &S.cons[warp + 1]; out.base = i * L;
     }
     int c = 0;
-    ok = sweep_job_band<KIND, R>(p16, P.sc, a_sym, b_sym, N, M, band * 32 * R, lane, in, out, W, c, tb);
+    ok = sweep_job_band<KIND, R>(p16, P.sc, a_sym, b_sym, N, M, band * 32 * R, lane, in, out, W, c, tb,
+                                 col_dst<KIND>(P, jb, band, lane));
     if (band == nb - 1) { corner = c; corner_band = band; }
   }
   // results: the corner from the warp that swept the last band, SW best over the CTA
@@ -585,9 +626,11 @@ __device__ void warp_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob 
     in.buf = row;
     Dst out;
     out.cons_seen = 0;
-    out.mode = band == nb - 1 ? OUT_NONE : OUT_OWN;
+    out.mode = OUT_OWN;
     out.buf = row;
-    if (!sweep_job_band<KIND, R>(p16, P.sc, a_sym, b_sym, N, M, band * 32 * R, lane, in, out, W, corner, tb))
+    if (band == nb - 1) last_row_dst<KIND>(P, jb, out);
+    if (!sweep_job_band<KIND, R>(p16, P.sc, a_sym, b_sym, N, M, band * 32 * R, lane, in, out, W, corner, tb,
+                                 col_dst<KIND>(P, jb, band, lane)))
       return;
   }
   if (KIND == K_SW) tb = warp_best(tb);
@@ -803,7 +846,8 @@ BatchTuning batch_tuning_for(const gme_pair *pairs, long long npairs, const Batc
 }
 
 int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long npairs,
-               long long nsym, const BatchTuning &tune_given, cudaStream_t st) {
+               long long nsym, const BatchTuning &tune_given, cudaStream_t st,
+               const long long *row_offs, const long long *col_offs) {
   constexpr int R = 4;
   const BatchTuning tune = batch_tuning_for(pairs, npairs, tune_given);
   const int NW = tune.warps_per_block;
@@ -848,7 +892,13 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
   std::sort(warpj.begin(), warpj.end(), by_cells);
   std::sort(teamj.begin(), teamj.end(), by_cells);
   ar.long_pairs.clear();
-  for (int i : ar.longj) ar.long_pairs.push_back(pairs[i]);
+  ar.long_rows.clear();
+  ar.long_cols.clear();
+  for (int i : ar.longj) {
+    ar.long_pairs.push_back(pairs[i]);
+    ar.long_rows.push_back(row_offs ? row_offs[i] : -1);
+    ar.long_cols.push_back(col_offs ? col_offs[i] : -1);
+  }
   // staged layout: a padded with PADL/PADR at a 16-byte aligned start, b padded to whole bands
   const long long nseg = 2 * (long long)(blockj.size() + warpj.size() + teamj.size());
   ar.h_from.resize(nseg); ar.h_to.resize(nseg); ar.h_len.resize(nseg); ar.h_padl.resize(nseg); ar.h_total.resize(nseg);
@@ -869,6 +919,8 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
     const int brows = (p.n2 + rows_mult - 1) / rows_mult * rows_mult;
     j.b_off = place(p.b_off, p.n2, 0, brows);
     j.n1 = p.n1; j.n2 = p.n2; j.kind = p.kind; j.index = (int)i;
+    j.row_off = row_offs ? row_offs[i] : -1;
+    j.col_off = col_offs ? col_offs[i] : -1;
     ar.h_jobs[slot] = j;
   };
   size_t slot = 0;
@@ -933,7 +985,8 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
 // work-queue kernel.  Stream operations only, so the sequence can be captured.
 // Returns the number of kernels launched in *kernels.
 int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring &sc,
-                 gme_result *d_results, cudaStream_t st, unsigned long long timeout_ns, int *kernels) {
+                 gme_result *d_results, cudaStream_t st, unsigned long long timeout_ns, int *kernels,
+                 int *d_last_rows, int *d_last_cols) {
   *kernels = 0;
   if (ar.nseg == 0) return ST_OK;
   cudaError_t e;
@@ -958,6 +1011,8 @@ int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring 
   P.twrap = reinterpret_cast<unsigned long long *>(ar.d_team + (long long)ar.n_t * sizeof(TeamSlot));
   P.results = d_results;
   P.done = ar.d_done;
+  P.last_rows = d_last_rows;
+  P.last_cols = d_last_cols;
   P.symbad = ar.d_symbad;
   P.packed16 = ar.packed16;
   P.rows = ar.d_rows;
@@ -974,13 +1029,15 @@ int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring 
 
 // Pairs the shared-memory rows cannot hold (or empty ones): the plain path, one
 // call each.  Never captured: the plain path hands out fresh band tags per call.
-int batch_long(BatchArena &ar, const int *d_sym, gme_result *d_results,
-               int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *),
+int batch_long(BatchArena &ar, const int *d_sym, gme_result *d_results, int *d_last_rows, int *d_last_cols,
+               int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *, int *, int *),
                void *plain_ctx) {
   for (size_t k = 0; k < ar.longj.size(); ++k) {
     const gme_pair &p = ar.long_pairs[k];
+    int *row = d_last_rows && ar.long_rows[k] >= 0 ? d_last_rows + ar.long_rows[k] : nullptr;
+    int *col = d_last_cols && ar.long_cols[k] >= 0 ? d_last_cols + ar.long_cols[k] : nullptr;
     const int rc = plain(plain_ctx, p.kind, d_sym + p.a_off, p.n1, d_sym + p.b_off, p.n2,
-                         d_results + ar.longj[k]);
+                         d_results + ar.longj[k], row, col);
     if (rc != ST_OK) return rc;
   }
   return ST_OK;
@@ -989,15 +1046,17 @@ int batch_long(BatchArena &ar, const int *d_sym, gme_result *d_results,
 int batch_run(Workspace &ws, BatchArena &ar, const int *d_sym, long long nsym, const gme_pair *pairs,
               long long npairs, const Scoring &sc, gme_result *d_results, cudaStream_t st,
               const BatchTuning &tune, unsigned long long timeout_ns,
-              int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *),
+              int *d_last_rows, const long long *row_offs, int *d_last_cols, const long long *col_offs,
+              int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *, int *, int *),
               void *plain_ctx) {
-  int rc = batch_plan(ws, ar, pairs, npairs, nsym, tune, st);
+  int rc = batch_plan(ws, ar, pairs, npairs, nsym, tune, st, d_last_rows ? row_offs : nullptr,
+                      d_last_cols ? col_offs : nullptr);
   if (rc != ST_OK) return rc;
   int k = 0;
-  rc = batch_launch(ws, ar, d_sym, sc, d_results, st, timeout_ns, &k);
+  rc = batch_launch(ws, ar, d_sym, sc, d_results, st, timeout_ns, &k, d_last_rows, d_last_cols);
   ws.launches += k;
   if (rc != ST_OK) return rc;
-  return batch_long(ar, d_sym, d_results, plain, plain_ctx);
+  return batch_long(ar, d_sym, d_results, d_last_rows, d_last_cols, plain, plain_ctx);
 }
 
 }  // namespace gme

@@ -46,6 +46,8 @@ struct BatchJob {
   int kind;
   int index;  // result slot
   int seg;    // staged segment of a (b is seg + 1): its symbols' range check
+  long long row_off = -1;  // last row (n1 + 1 values) at last_rows + row_off, or none
+  long long col_off = -1;  // last column (n2 + 1 values) at last_cols + col_off, or none
 };
 
 struct BatchTuning {
@@ -96,6 +98,7 @@ struct BatchArena {
   int kb[4] = {0, 0, 0, 0}, kw[4] = {0, 0, 0, 0};  // per-kind offsets into the two queues
   std::vector<int> longj;             // result slots of pairs for the plain path
   std::vector<gme_pair> long_pairs;   // their descriptors
+  std::vector<long long> long_rows, long_cols;  // their last-row / last-column offsets (-1: none)
   bool sync_before_reuse = true;      // wait for the stream before overwriting the plan
   int reserve(long long staged, long long nseg, long long njobs, Workspace &ws);
   int reserve_rows(long long ints, Workspace &ws);
@@ -112,16 +115,19 @@ long long batch_pair_bytes(long long n1, long long n2);
 long long batch_grid(int sms, int NW, int blocks_per_sm);
 long long batch_scratch_bytes(long long grid, int NW, int max_n1);
 int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long npairs,
-               long long nsym, const BatchTuning &tune, cudaStream_t st);
+               long long nsym, const BatchTuning &tune, cudaStream_t st,
+               const long long *row_offs = nullptr, const long long *col_offs = nullptr);
 int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring &sc,
-                 gme_result *d_results, cudaStream_t st, unsigned long long timeout_ns, int *kernels);
-int batch_long(BatchArena &ar, const int *d_sym, gme_result *d_results,
-               int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *),
+                 gme_result *d_results, cudaStream_t st, unsigned long long timeout_ns, int *kernels,
+                 int *d_last_rows = nullptr, int *d_last_cols = nullptr);
+int batch_long(BatchArena &ar, const int *d_sym, gme_result *d_results, int *d_last_rows, int *d_last_cols,
+               int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *, int *, int *),
                void *plain_ctx);
 int batch_run(Workspace &ws, BatchArena &ar, const int *d_sym, long long nsym, const gme_pair *pairs,
               long long npairs, const Scoring &sc, gme_result *d_results, cudaStream_t st,
               const BatchTuning &tune, unsigned long long timeout_ns,
-              int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *),
+              int *d_last_rows, const long long *row_offs, int *d_last_cols, const long long *col_offs,
+              int (*plain)(void *, int, const int *, long long, const int *, long long, gme_result *, int *, int *),
               void *plain_ctx);
 
 // plain path (gme_plain.cu)

@@ -6,8 +6,10 @@
 // row G of the table of the two reversed remainders (a[i0, i1) and b[m, j1) read
 // backwards) give, for each column k, the best score of a path through (m, k):
 // F[k] + G[cols - k].  The best k splits the problem into (a[i0, i0+k), b[j0, m)) and
-// (a[i0+k, i1), b[m, j1)), which are solved the same way, level by level (every node
-// of a level is queued on the stream, one copy brings the split columns back).
+// (a[i0+k, i1), b[m, j1)), which are solved the same way, level by level: all halves
+// of a level go to the GPU as one batch (gme_align_batch_device_rows, each half's
+// last row written at its offset), one kernel picks every node's split, and one copy
+// brings the split columns back.
 // Subproblems of at most LEAF_ROWS rows and LEAF_CELLS cells are solved whole, one
 // CTA each in a single launch: an anti-diagonal sweep that keeps 2-bit directions in
 // shared memory, then the walk back from the corner.
@@ -42,17 +44,32 @@ struct Leaf {
   long long out;  // offset of its script in the ops buffer (rows + cols characters)
 };
 
-// Reverses `n` symbols of src into dst.
-__global__ void reverse_kernel(const int *__restrict__ src, int *__restrict__ dst, int n) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    dst[i] = src[n - 1 - i];
+// One inner node of a level: its two halves' last rows and where its split goes.
+struct NodeJob {
+  long long F, G;  // offsets of the forward and backward last rows (cols + 1 values each)
+  int cols;
+};
+
+// Reverses segment s (len[s] symbols at src[s]) into dst[s], one CTA per segment.
+__global__ void reverse_kernel(int *__restrict__ sym, const long long *__restrict__ src,
+                               const long long *__restrict__ dst, const int *__restrict__ len, int nseg) {
+  for (int s = blockIdx.x; s < nseg; s += gridDim.x) {
+    const int n = len[s];
+    const int *from = sym + src[s];
+    int *to = sym + dst[s];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) to[i] = from[n - 1 - i];
+  }
 }
 
-// The best split column of a node: k in [0, cols] optimising F[k] + G[cols - k]
-// (ED: the smallest sum, LCS: the largest), the smallest k among equals.
-__global__ void split_kernel(const int *__restrict__ F, const int *__restrict__ G, int cols, int kind,
+// The best split column of each node (one CTA per node): k in [0, cols] optimising
+// F[k] + G[cols - k] (ED: the smallest sum, LCS: the largest), the smallest k among
+// equals.
+__global__ void split_kernel(const int *__restrict__ rows, const NodeJob *__restrict__ nodes, int kind,
                              int *__restrict__ out) {
   __shared__ long long best[32];
+  const NodeJob nd = nodes[blockIdx.x];
+  const int *F = rows + nd.F, *G = rows + nd.G;
+  const int cols = nd.cols;
   long long b = LLONG_MAX;
   for (int k = threadIdx.x; k <= cols; k += blockDim.x) {
     const long long s = (long long)F[k] + G[cols - k];
@@ -65,7 +82,7 @@ __global__ void split_kernel(const int *__restrict__ F, const int *__restrict__ 
   if (threadIdx.x == 0) {
     long long m = best[0];
     for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = min(m, best[w]);
-    *out = (int)(m & 0xffffff);
+    out[blockIdx.x] = (int)(m & 0xffffff);
   }
 }
 
@@ -147,6 +164,7 @@ __global__ void __launch_bounds__(LEAF_ROWS) leaf_kernel(const int *__restrict__
 
 using gme::Leaf;
 using gme::PathNode;
+using gme::NodeJob;
 
 extern "C" gme_status gme_align_path(gme_context *ctx, gme_kind kind, const int32_t *a, int64_t n1,
                                      const int32_t *b, int64_t n2, const gme_scoring *sc, char *ops,
@@ -165,20 +183,22 @@ extern "C" gme_status gme_align_path(gme_context *ctx, gme_kind kind, const int3
     if (st) cudaStreamDestroy(st);
     return rc;
   };
-  // device copies of both sequences (forward) and scratch for reversed remainders
-  int *d_a = nullptr, *d_b = nullptr, *d_ra = nullptr, *d_rb = nullptr, *d_F = nullptr, *d_G = nullptr;
-  int *d_split = nullptr;
+  // one symbol buffer: a, then b, then the reversed remainders of a level
+  const long long sym_len = 2 * (n1 + n2) + 16;
+  int *d_sym = nullptr, *d_rows = nullptr, *d_split = nullptr;
   gme_result *d_res = nullptr;
+  long long *d_rsrc = nullptr, *d_rdst = nullptr;
+  int *d_rlen = nullptr;
+  NodeJob *d_nodes = nullptr;
   auto release = [&] {
-    cudaFree(d_a); cudaFree(d_b); cudaFree(d_ra); cudaFree(d_rb); cudaFree(d_F); cudaFree(d_G);
-    cudaFree(d_split); cudaFree(d_res);
+    cudaFree(d_sym); cudaFree(d_rows); cudaFree(d_split); cudaFree(d_res);
+    cudaFree(d_rsrc); cudaFree(d_rdst); cudaFree(d_rlen); cudaFree(d_nodes);
   };
-  const size_t na = (size_t)std::max<int64_t>(n1, 1), nb = (size_t)std::max<int64_t>(n2, 1);
-  if (cudaMalloc(&d_a, na * 4) || cudaMalloc(&d_b, nb * 4) || cudaMalloc(&d_ra, na * 4) ||
-      cudaMalloc(&d_rb, nb * 4) || cudaMalloc(&d_res, sizeof(gme_result) * 2)) {
+  if (cudaMalloc(&d_sym, (size_t)sym_len * 4) || cudaMalloc(&d_res, sizeof(gme_result))) {
     release();
     return fail(GME_ERR_NOMEM);
   }
+  int *d_a = d_sym, *d_b = d_sym + n1;
   if (n1) cudaMemcpyAsync(d_a, a, (size_t)n1 * 4, cudaMemcpyHostToDevice, st);
   if (n2) cudaMemcpyAsync(d_b, b, (size_t)n2 * 4, cudaMemcpyHostToDevice, st);
   // the optimal score, from the score-only path
@@ -206,6 +226,7 @@ extern "C" gme_status gme_align_path(gme_context *ctx, gme_kind kind, const int3
   tree.push_back({-1, -1, -1});
   long long ops_total = 0;
   gme_status rc = GME_OK;
+  long long rows_cap = 0, nodes_cap = 0;
   while (!level.empty() && rc == GME_OK) {
     std::vector<PathNode> inner;
     std::vector<int> inner_ids;
@@ -222,39 +243,72 @@ extern "C" gme_status gme_align_path(gme_context *ctx, gme_kind kind, const int3
       }
     }
     if (inner.empty()) break;
-    // queue every inner node: forward half, reversed remainders, backward half, split
-    long long need = 0;
-    for (const PathNode &p : inner) need += (p.i1 - p.i0) + 1;
-    cudaFree(d_F); cudaFree(d_G); cudaFree(d_split);
-    d_F = d_G = d_split = nullptr;
-    if (cudaMalloc(&d_F, need * 4) || cudaMalloc(&d_G, need * 4) || cudaMalloc(&d_split, inner.size() * 4)) {
-      rc = GME_ERR_NOMEM;
-      break;
-    }
-    long long off = 0;
-    for (size_t k = 0; k < inner.size() && rc == GME_OK; ++k) {
+    // the level's batch: per node, its top half forward and its bottom half reversed
+    const long long nn = (long long)inner.size();
+    std::vector<gme_pair> pairs(2 * nn);
+    std::vector<int64_t> row_off(2 * nn);
+    std::vector<NodeJob> nodes(nn);
+    std::vector<long long> rsrc, rdst;
+    std::vector<int> rlen;
+    long long roff = 0, rev = n1 + n2;
+    for (long long k = 0; k < nn; ++k) {
       const PathNode &p = inner[k];
-      const int cols = p.i1 - p.i0, m = p.j0 + (p.j1 - p.j0) / 2;
-      rc = gme_align_device(ctx, kind, d_a + p.i0, cols, d_b + p.j0, m - p.j0, &s, d_res, d_F + off, nullptr, st);
-      if (rc != GME_OK) break;
-      if (cols) gme::reverse_kernel<<<std::min(1024, (cols + 255) / 256), 256, 0, st>>>(d_a + p.i0, d_ra, cols);
-      if (p.j1 - m)
-        gme::reverse_kernel<<<std::min(1024, (p.j1 - m + 255) / 256), 256, 0, st>>>(d_b + m, d_rb, p.j1 - m);
-      rc = gme_align_device(ctx, kind, d_ra, cols, d_rb, p.j1 - m, &s, d_res + 1, d_G + off, nullptr, st);
-      if (rc != GME_OK) break;
-      gme::split_kernel<<<1, 1024, 0, st>>>(d_F + off, d_G + off, cols, (int)kind, d_split + k);
-      off += cols + 1;
+      const int cols = p.i1 - p.i0, m = p.j0 + (p.j1 - p.j0) / 2, rb = p.j1 - m;
+      pairs[2 * k] = gme_pair{(int64_t)p.i0, (int64_t)(n1 + p.j0), cols, m - p.j0, (int32_t)kind, 0};
+      rsrc.push_back(p.i0); rdst.push_back(rev); rlen.push_back(cols);
+      rsrc.push_back(n1 + m); rdst.push_back(rev + cols); rlen.push_back(rb);
+      pairs[2 * k + 1] = gme_pair{(int64_t)rev, (int64_t)(rev + cols), cols, rb, (int32_t)kind, 0};
+      rev += cols + rb;
+      nodes[k] = {roff, roff + cols + 1, cols};
+      row_off[2 * k] = roff;
+      row_off[2 * k + 1] = roff + cols + 1;
+      roff += 2 * (long long)(cols + 1);
     }
-    if (rc != GME_OK) break;
-    std::vector<int> split(inner.size());
-    if (cudaMemcpyAsync(split.data(), d_split, inner.size() * 4, cudaMemcpyDeviceToHost, st) ||
-        cudaStreamSynchronize(st)) {
+    if (roff > rows_cap) {
+      cudaFree(d_rows);
+      d_rows = nullptr;
+      rows_cap = roff + roff / 4;
+      if (cudaMalloc(&d_rows, (size_t)rows_cap * 4)) { rc = GME_ERR_NOMEM; break; }
+    }
+    if (nn > nodes_cap) {
+      cudaFree(d_split); cudaFree(d_nodes); cudaFree(d_rsrc); cudaFree(d_rdst); cudaFree(d_rlen);
+      d_split = nullptr; d_nodes = nullptr; d_rsrc = d_rdst = nullptr; d_rlen = nullptr;
+      nodes_cap = nn + nn / 4 + 16;
+      if (cudaMalloc(&d_split, nodes_cap * 4) || cudaMalloc(&d_nodes, nodes_cap * sizeof(NodeJob)) ||
+          cudaMalloc(&d_rsrc, 2 * nodes_cap * 8) || cudaMalloc(&d_rdst, 2 * nodes_cap * 8) ||
+          cudaMalloc(&d_rlen, 2 * nodes_cap * 4)) {
+        rc = GME_ERR_NOMEM;
+        break;
+      }
+    }
+    // pageable sources: each copy has taken its bytes before it returns
+    cudaMemcpyAsync(d_rsrc, rsrc.data(), rsrc.size() * 8, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_rdst, rdst.data(), rdst.size() * 8, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_rlen, rlen.data(), rlen.size() * 4, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_nodes, nodes.data(), nodes.size() * sizeof(NodeJob), cudaMemcpyHostToDevice, st);
+    gme::reverse_kernel<<<(unsigned)std::min<long long>(2 * nn, 65535), 256, 0, st>>>(d_sym, d_rsrc, d_rdst,
+                                                                                    d_rlen, (int)(2 * nn));
+    gme_result *d_lres = nullptr;
+    if (cudaMalloc(&d_lres, 2 * nn * sizeof(gme_result))) { rc = GME_ERR_NOMEM; break; }
+    rc = gme_align_batch_device_rows(ctx, d_sym, sym_len, pairs.data(), 2 * nn, &s, d_lres, d_rows,
+                                     row_off.data(), nullptr, nullptr, st);
+    if (rc == GME_OK) {
+      gme::split_kernel<<<(unsigned)nn, 256, 0, st>>>(d_rows, d_nodes, (int)kind, d_split);
+    }
+    std::vector<int> split(nn);
+    std::vector<gme_result> lres(2 * nn);
+    if (rc == GME_OK && (cudaMemcpyAsync(split.data(), d_split, nn * 4, cudaMemcpyDeviceToHost, st) ||
+                         cudaMemcpyAsync(lres.data(), d_lres, 2 * nn * sizeof(gme_result),
+                                         cudaMemcpyDeviceToHost, st) ||
+                         cudaStreamSynchronize(st)))
       rc = GME_ERR_CUDA;
-      break;
-    }
+    cudaFree(d_lres);
+    for (const gme_result &r : lres)
+      if (rc == GME_OK && r.status != 0) rc = (gme_status)r.status;  // a wait gave up: no path
+    if (rc != GME_OK) break;
     std::vector<PathNode> next;
     std::vector<int> next_ids;
-    for (size_t k = 0; k < inner.size(); ++k) {
+    for (long long k = 0; k < nn; ++k) {
       const PathNode &p = inner[k];
       const int m = p.j0 + (p.j1 - p.j0) / 2, c = p.i0 + split[k];
       const int l = (int)tree.size(), r = l + 1;

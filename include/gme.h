@@ -159,6 +159,16 @@ gme_status gme_align_batch(gme_context *ctx, const int32_t *symbols, int64_t nsy
 gme_status gme_align_batch_device(gme_context *ctx, const int32_t *d_symbols, int64_t nsym,
                                   const gme_pair *pairs, int64_t npairs, const gme_scoring *sc,
                                   gme_result *d_results, void *stream);
+/* As gme_align_batch_device, and each pair's boundary as well: pair i's last row
+ * (row n2, n1+1 values) at d_last_rows + row_offsets[i] and its last column (column
+ * n1, n2+1 values) at d_last_cols + col_offsets[i], as the plain path returns them.
+ * An offset of -1 skips that pair; either buffer may be NULL (then its offsets are
+ * not read).  Offsets are element offsets in host arrays of npairs entries. */
+gme_status gme_align_batch_device_rows(gme_context *ctx, const int32_t *d_symbols, int64_t nsym,
+                                       const gme_pair *pairs, int64_t npairs, const gme_scoring *sc,
+                                       gme_result *d_results, int32_t *d_last_rows,
+                                       const int64_t *row_offsets, int32_t *d_last_cols,
+                                       const int64_t *col_offsets, void *stream);
 /* A reusable plan for a fixed pair list: classification, ordering, staged layout
  * and descriptors are made once; each run only clears the tickets, stages the
  * symbols and launches the work-queue kernel.  With use_graph != 0 the first run

@@ -155,6 +155,67 @@ def test_engine_selection(gme_ctx, packed16):
         gme_ctx.set_batch_config()
 
 
+@pytest.mark.parametrize("rule,packed16", [(0, 1), (1, 1), (1, -1)])
+def test_batch_last_rows_and_columns(gme_ctx, rule, packed16):
+    """Each pair's last row and last column from one batch, as the plain path gives them:
+    warp, block and team jobs, both engines, pairs on the plain path, pairs skipped."""
+    import torch
+    import gpumemefficient_gb300 as g
+    rng = np.random.default_rng(808 + rule)
+    kinds, sa, sb = [], [], []
+    shapes = [(int(rng.integers(1, 3000)), int(rng.integers(1, 3000))) for _ in range(80)]
+    shapes += [(16384, 300), (17000, 100), (9000, 4000), (0, 5), (6, 0), (3000, 9000)]
+    for i, (n1, n2) in enumerate(shapes):
+        kinds.append(i % 3)
+        sa.append(rng.integers(0, 4, n1))
+        sb.append(rng.integers(0, 4, n2))
+    symbols, pairs = g.pack_batch(kinds, sa, sb)
+    n = len(pairs)
+    row_off = np.full(n, -1, np.int64)
+    col_off = np.full(n, -1, np.int64)
+    r = c = 0
+    for i in range(n):
+        if i % 7 != 3:
+            row_off[i] = r
+            r += len(sa[i]) + 1
+        if i % 5 != 2:
+            col_off[i] = c
+            c += len(sb[i]) + 1
+    dev = torch.device("cuda", 0)
+    d_sym = torch.from_numpy(symbols).to(dev)
+    d_res = torch.zeros(n * g.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    d_rows = torch.full((max(r, 1),), -7, dtype=torch.int32, device=dev)
+    d_cols = torch.full((max(c, 1),), -7, dtype=torch.int32, device=dev)
+    sc = g.scoring(ed_boundary=rule)
+    gme_ctx.set_batch_config(team_min_cells=1 << 20, block_min_cells=1 << 20, packed16=packed16)
+    try:
+        gme_ctx.align_batch_device_rows(d_sym.data_ptr(), len(symbols), pairs, d_res.data_ptr(),
+                                        d_rows.data_ptr(), row_off, d_cols.data_ptr(), col_off, sc=sc)
+        torch.cuda.synchronize()
+        st = gme_ctx.batch_stats()
+    finally:
+        gme_ctx.set_batch_config()
+    assert st["team_jobs"] > 0 and st["block_jobs"] > 0 and st["warp_jobs"] > 0 and st["long_jobs"] > 0
+    res = np.frombuffer(d_res.cpu().numpy().tobytes(), g.RESULT_DTYPE)
+    rows = d_rows.cpu().numpy()
+    cols = d_cols.cpu().numpy()
+    for i in range(n):
+        o = O.align(kinds[i], sa[i], sb[i], rule=rule)
+        assert res["status"][i] == 0 and res["score"][i] == o["score"], i
+        if row_off[i] >= 0:
+            np.testing.assert_array_equal(rows[row_off[i]:row_off[i] + len(sa[i]) + 1], o["last_row"],
+                                          err_msg=f"pair {i} row")
+        if col_off[i] >= 0:
+            np.testing.assert_array_equal(cols[col_off[i]:col_off[i] + len(sb[i]) + 1], o["last_col"],
+                                          err_msg=f"pair {i} col")
+    # skipped pairs leave the buffers alone
+    used_r = np.zeros(len(rows), bool)
+    for i in range(n):
+        if row_off[i] >= 0:
+            used_r[row_off[i]:row_off[i] + len(sa[i]) + 1] = True
+    assert (rows[~used_r] == -7).all()
+
+
 def test_identical_and_disjoint(gme_ctx):
     rng = np.random.default_rng(5)
     kinds, sa, sb = [], [], []
