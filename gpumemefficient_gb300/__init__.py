@@ -58,7 +58,7 @@ class BatchConfig(ctypes.Structure):
     _fields_ = [("warps_per_block", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("block_min_cells", ctypes.c_int64), ("long_min_cells", ctypes.c_int64),
                 ("team_min_cells", ctypes.c_int64), ("packed16", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("team_split", ctypes.c_int32)]
 
 
 PAIR_DTYPE = np.dtype([("a_off", "<i8"), ("b_off", "<i8"), ("n1", "<i4"), ("n2", "<i4"),
@@ -244,9 +244,9 @@ class Context:
 
     def set_batch_config(self, warps_per_block: int = 0, blocks_per_sm: int = 0,
                          block_min_cells: int = 0, long_min_cells: int = 0, team_min_cells: int = 0,
-                         packed16: int = 0):
+                         packed16: int = 0, team_split: int = 0):
         cfg = BatchConfig(warps_per_block, blocks_per_sm, block_min_cells, long_min_cells, team_min_cells,
-                          int(packed16), 0)
+                          int(packed16), team_split)
         _check(lib().gme_set_batch_config(self.handle, ctypes.byref(cfg)), self.handle)
 
     def batch_stats(self) -> dict:
@@ -374,14 +374,18 @@ class Server:
         return t.value
 
     def submit_many(self, symbols: np.ndarray, pairs: np.ndarray) -> np.ndarray:
-        """Queues len(pairs) alignments (PAIR_DTYPE over one int32 symbol buffer); returns tickets."""
+        """Queues alignments (PAIR_DTYPE over one int32 symbol buffer); returns the tickets
+        of those queued: all of them, or a prefix when the queue is full (the caller
+        submits the rest later)."""
         symbols = np.ascontiguousarray(symbols, np.int32)
         pairs = np.ascontiguousarray(pairs, PAIR_DTYPE)
         tickets = np.zeros(len(pairs), np.uint64)
         k = ctypes.c_int64()
-        self._err(lib().gme_submit_many(self.handle, symbols.ctypes.data, pairs.ctypes.data, len(pairs),
-                                        tickets.ctypes.data, ctypes.byref(k)))
-        return tickets
+        st = lib().gme_submit_many(self.handle, symbols.ctypes.data, pairs.ctypes.data, len(pairs),
+                                   tickets.ctypes.data, ctypes.byref(k))
+        if st != self.NOT_READY:
+            self._err(st)
+        return tickets[:k.value]
 
     def poll(self, ticket: int):
         """(result dict, latency_ns) once done, else None."""

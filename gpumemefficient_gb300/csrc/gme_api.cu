@@ -437,18 +437,19 @@ gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg) {
       t.warps_per_block = cfg->warps_per_block;
     }
     if (cfg->blocks_per_sm < 0 || cfg->block_min_cells < 0 || cfg->long_min_cells < -1 ||
-        cfg->team_min_cells < -1)
+        cfg->team_min_cells < -1 || cfg->team_split < 0)
       return GME_ERR_INVALID;
     t.blocks_per_sm = cfg->blocks_per_sm;
     if (cfg->block_min_cells) t.block_min_cells = cfg->block_min_cells;
     t.long_min_cells = cfg->long_min_cells;
     if (cfg->team_min_cells) t.team_min_cells = cfg->team_min_cells;
+    if (cfg->team_split) t.team_split = cfg->team_split;
     if (cfg->packed16 < -1 || cfg->packed16 > 1) return GME_ERR_INVALID;
     t.packed16 = cfg->packed16 >= 0;
   }
   // an all-zero configuration means "automatic" (the tuned table)
   t.user_set = cfg && (cfg->warps_per_block || cfg->blocks_per_sm || cfg->block_min_cells ||
-                       cfg->long_min_cells || cfg->team_min_cells);
+                       cfg->long_min_cells || cfg->team_min_cells || cfg->team_split);
   if (!t.user_set && cfg) t.packed16 = cfg->packed16 >= 0;
   ctx->batch_tune = t;
   return GME_OK;

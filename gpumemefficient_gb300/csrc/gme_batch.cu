@@ -27,13 +27,19 @@
 
 namespace gme {
 
-// Wavefront steps per ring transaction in this kernel.  Shorter than the plain
-// kernel's: a dozen independent warps per SM each run their own pair at their own
-// point in the loop, so the loop body must stay small for the instruction cache.
+// Wavefront steps per ring transaction in this kernel.  A dozen independent warps
+// per SM each run their own pair at their own point in the loop, so the loop body
+// must stay small for the instruction cache; with one chunk body per kind and engine
+// 16 steps fit and halve the per-chunk ring and tag work against 8.
 #ifndef GME_BATCH_CHUNK
-#define GME_BATCH_CHUNK 8
+#define GME_BATCH_CHUNK 16
 #endif
 constexpr int CB = GME_BATCH_CHUNK;
+// Resident 4-warp CTAs per SM the register allocation is sized for (65536 registers
+// / (128 threads x 3) caps a thread at 168).
+#ifndef GME_BATCH_MIN_BLOCKS
+#define GME_BATCH_MIN_BLOCKS 3
+#endif
 
 
 constexpr int BATCH_MAXN = BATCH_MAX_N1;
@@ -651,7 +657,7 @@ __device__ void warp_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob 
 }
 
 template <int R, int NW>
-__global__ void __launch_bounds__(NW * 32, NW == 4 ? 3 : 1) batch_kernel(BatchParams P) {
+__global__ void __launch_bounds__(NW * 32, NW == 4 ? GME_BATCH_MIN_BLOCKS : 1) batch_kernel(BatchParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   BatchSmem<NW> &S = *reinterpret_cast<BatchSmem<NW> *>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -660,8 +666,17 @@ __global__ void __launch_bounds__(NW * 32, NW == 4 ? 3 : 1) batch_kernel(BatchPa
   Waiter W(P.timeout_ns, &P.ctrl[8], &S.abort);
   // One kind after another, so that an SM runs one kind's code at a time (the
   // three kinds' loops do not fit the instruction cache together); within a kind
-  // first the large pairs one per CTA, then the rest one per warp.
-  for (int k = 0; k < 3; ++k) {
+  // first the large pairs one per CTA, then the rest one per warp.  Each pair of
+  // SMs starts at kind (smid / 2) % 3, so that the largest pairs of every kind start
+  // at once instead of the last kind's at the end of the batch.  Measured: the two
+  // SMs of a pair behave as sharing an instruction cache (starting each single SM at
+  // its own kind lost 40%, each pair +10% on the 16384-pair batch, +17% on the
+  // [32, 16384] mix).
+  unsigned smid;
+  asm("mov.u32 %0, %%smid;" : "=r"(smid));
+  const int kfirst = (int)((smid >> 1) % 3u);
+  for (int kk = 0; kk < 3; ++kk) {
+    const int k = kfirst + kk < 3 ? kfirst + kk : kfirst + kk - 3;
     const int b0 = P.kb[k], nb = P.kb[k + 1] - b0, w0 = P.kw[k], nw = P.kw[k + 1] - w0;
     const int u0 = P.ku[k], nu = P.ku[k + 1] - u0;
     // phase 1: members of team jobs (claimed in order, so a member waits only on
@@ -842,6 +857,7 @@ BatchTuning batch_tuning_for(const gme_pair *pairs, long long npairs, const Batc
   t.blocks_per_sm = TUNED[best].blocks_per_sm;
   t.block_min_cells = TUNED[best].block_min_cells;
   t.team_min_cells = TUNED[best].team_min_cells;
+  t.team_split = TUNED[best].team_split;
   return t;
 }
 
@@ -890,6 +906,8 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
   };
   std::sort(blockj.begin(), blockj.end(), by_cells);
   std::sort(warpj.begin(), warpj.end(), by_cells);
+  // team jobs kind by kind as well: claiming every kind's teams first put the three
+  // kinds' loops on one SM at once and halved the throughput of the [32, 16384] mix
   std::sort(teamj.begin(), teamj.end(), by_cells);
   ar.long_pairs.clear();
   ar.long_rows.clear();
@@ -926,12 +944,12 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
   size_t slot = 0;
   for (int i : blockj) add(i, 32 * R * NW, slot++);
   for (int i : warpj) add(i, 32 * R, slot++);
-  // a team of T = groups/2 (2..8) CTAs per team job; members claimed in order
+  // a team of T = groups / team_split (2..8) CTAs per team job; members claimed in order
   ar.h_units.clear();
   for (size_t j = 0; j < teamj.size(); ++j) {
     add(teamj[j], 32 * R * NW, slot++);
     const int G = (int)groups(pairs[teamj[j]]);
-    const int T = std::max(2, std::min(8, G / 2));
+    const int T = std::max(2, std::min(8, G / std::max(1, tune.team_split)));
     for (int t = 0; t < T; ++t) ar.h_units.push_back(make_int4((int)j, t, T, 0));
   }
   cudaError_t e;

@@ -60,6 +60,8 @@ struct BatchTuning {
   long long long_min_cells = 0;
   // pairs at least this large (with 4+ band groups) run on a team of CTAs; < 0 = never
   long long team_min_cells = 1ll << 25;
+  // a team job of G band groups runs on clamp(G / team_split, 2, 8) CTAs
+  int team_split = 2;
   // pairs whose values fit 16 bits run on the packed 16-bit engine
   bool packed16 = true;
   // false: the plan takes warps, CTAs per SM and cut-offs from the tuned table

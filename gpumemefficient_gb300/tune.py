@@ -53,23 +53,44 @@ GRID = {
     "blocks_per_sm": [0, 2],
     "block_min_cells": [1 << 20, 1 << 21, 1 << 22, 1 << 23],
     "team_min_cells": [1 << 24, 1 << 25, 1 << 26, -1],
+    "team_split": [2, 3, 4],
 }
 QUICK_GRID = {
     "warps_per_block": [4, 8],
     "blocks_per_sm": [0],
     "block_min_cells": [1 << 21, 1 << 22],
     "team_min_cells": [1 << 25, -1],
+    "team_split": [2],
 }
+
+
+def lengths_for(lo: int, hi: int, cells: float, rng):
+    """Lengths of a and b, log-uniform in [lo, hi], for about `cells` cells."""
+    mean = ((hi - lo) / np.log(hi / lo)) ** 2
+    n = int(min(40000, max(64, cells / mean)))
+    la = np.exp(rng.uniform(np.log(lo), np.log(hi), n)).astype(np.int64)
+    lb = np.exp(rng.uniform(np.log(lo), np.log(hi), n)).astype(np.int64)
+    return la, lb
+
+
+def length_range(la, lb):
+    """The statistic the batch plan matches table entries by (batch_tuning_for): the
+    2nd and 98th percentile of sqrt(n1 * n2) + 1 over the batch's pairs."""
+    v = np.sort(np.sqrt(la.astype(np.float64) * lb) + 1.0)
+    n = len(v)
+    return float(v[int(0.02 * (n - 1))]), float(v[int(0.98 * (n - 1))])
+
+
+def bucket_range(lo: int, hi: int, cells: float, seed: int):
+    return length_range(*lengths_for(lo, hi, cells, np.random.default_rng(seed)))
 
 
 def batch_for(lo: int, hi: int, cells: float, seed: int):
     """Seeded pairs with lengths log-uniform in [lo, hi] until about `cells` cells."""
     from . import pack_batch
     rng = np.random.default_rng(seed)
-    mean = ((hi - lo) / np.log(hi / lo)) ** 2
-    n = int(min(40000, max(64, cells / mean)))
-    la = np.exp(rng.uniform(np.log(lo), np.log(hi), n)).astype(np.int64)
-    lb = np.exp(rng.uniform(np.log(lo), np.log(hi), n)).astype(np.int64)
+    la, lb = lengths_for(lo, hi, cells, rng)
+    n = len(la)
     kinds = np.repeat(np.arange(3, dtype=np.int32), (n + 2) // 3)[:n]
     rng.shuffle(kinds)
     sa = [rng.integers(0, 4, int(k), dtype=np.int64).astype(np.int32) for k in la]
@@ -114,17 +135,21 @@ def sweep(grid=None, cells: float = 1.5e10, reps: int = 5, device: int = 0, log=
     rows = []
     for bi, (name, lo, hi) in enumerate(BUCKETS + MIXES):
         symbols, pairs, total = batch_for(lo, hi, cells, 0x5EED + bi)
+        p_lo, p_hi = bucket_range(lo, hi, cells, 0x5EED + bi)
         d_sym = torch.from_numpy(symbols).to(dev)
         d_res = torch.zeros(len(pairs) * RESULT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
         ref = None
         for vals in itertools.product(*(grid[k] for k in keys)):
             cfg = dict(zip(keys, vals))
+            if cfg.get("team_min_cells") == -1 and cfg.get("team_split", 2) != grid.get("team_split", [2])[0]:
+                continue  # no teams: the split changes nothing
             ms, split, res = measure(ctx, d_sym, d_res, pairs, len(symbols), cfg, reps, stream)
             ok = bool((res["status"] == 0).all())
             if ref is None:
                 ref = res
             same = bool((res["score"] == ref["score"]).all() and (res["sw_max"] == ref["sw_max"]).all())
-            row = {"bucket": name, "lo": lo, "hi": hi, "pairs": len(pairs), "cells": total, **cfg,
+            row = {"bucket": name, "lo": lo, "hi": hi, "p_lo": p_lo, "p_hi": p_hi, "pairs": len(pairs),
+                   "cells": total, **cfg,
                    "ms": ms, "gcups": total / ms / 1e6, "split": split, "ok": ok and same}
             rows.append(row)
             log(json.dumps(row))
@@ -150,47 +175,56 @@ def write_md(rows, best, path, cmd):
              f"Command (GB300): `{cmd}`", "",
              "GCUPS of one planned launch (CUDA-graph replay, CUDA events, mean of the replays) "
              "per length bucket; lengths log-uniform in [lo, hi], LCS/ED/SW one third each. "
-             "`team_min_cells` -1 = no teams. Every row's results equal the first row's.", ""]
+             "`team_min_cells` -1 = no teams; groups/member: a team job of G band groups runs on "
+             "clamp(G / that, 2, 8) CTAs. Every row's results equal the first row's. The match range "
+             "is the statistic the plan picks a table entry by: the 2nd..98th percentile of "
+             "sqrt(n1*n2)+1 over the bucket's pairs.", ""]
     for name in [b[0] for b in BUCKETS + MIXES]:
         rs = [r for r in rows if r["bucket"] == name]
         if not rs:
             continue
         w = best.get(name)
+        rng_txt = f", match range [{rs[0]['p_lo']:.0f}, {rs[0]['p_hi']:.0f}]" if "p_lo" in rs[0] else ""
         lines.append(f"## {name}: lengths [{rs[0]['lo']}, {rs[0]['hi']}], {rs[0]['pairs']} pairs, "
-                     f"{rs[0]['cells']:.3g} cells")
+                     f"{rs[0]['cells']:.3g} cells{rng_txt}")
         lines.append("")
-        lines.append("| warps/CTA | CTAs/SM | block_min | team_min | ms | GCUPS | split (team/block/warp/plain) | |")
-        lines.append("|---:|---:|---:|---:|---:|---:|---|---|")
+        lines.append("| warps/CTA | CTAs/SM | block_min | team_min | groups/member | ms | GCUPS | split (team/block/warp/plain) | |")
+        lines.append("|---:|---:|---:|---:|---:|---:|---:|---|---|")
         for r in sorted(rs, key=lambda r: -r["gcups"]):
             s = r["split"]
-            mark = "best" if r is w else ("" if r["ok"] else "MISMATCH")
+            mark = "best" if r == w else ("" if r["ok"] else "MISMATCH")
             lines.append(f"| {r['warps_per_block']} | {r['blocks_per_sm'] or 'max'} | 2^{int(np.log2(r['block_min_cells']))} | "
                          f"{('2^%d' % int(np.log2(r['team_min_cells']))) if r['team_min_cells'] > 0 else 'none'} | "
-                         f"{r['ms']:.3f} | {r['gcups']:.1f} | {s.get('team_jobs', 0)}/{s['block_jobs']}/{s['warp_jobs']}/{s['long_jobs']} | {mark} |")
+                         f"{r.get('team_split', 2)} | {r['ms']:.3f} | {r['gcups']:.1f} | {s.get('team_jobs', 0)}/{s['block_jobs']}/{s['warp_jobs']}/{s['long_jobs']} | {mark} |")
         lines.append("")
     with open(path, "w") as f:
         f.write("\n".join(lines))
 
 
-def gen_header(best, path=TUNED_H):
-    """The winners per bucket (and per mix) as the table the batch plan reads."""
+def gen_header(best, path=TUNED_H, cells: float = 1.5e10):
+    """The winners per bucket (and per mix) as the table the batch plan reads; each
+    entry's range is its own sweep batch's statistic (length_range)."""
     keys = [b for b in BUCKETS + MIXES if b[0] in best]
     out = ["// gme_tuned.h -- batched-kernel settings per length range, written by",
            "// gpumemefficient_gb300/tune.py from a sweep on GB300 (the sweep table is kept",
-           "// beside the profiles).  A batch is planned with the entry whose length range",
-           "// [lo, hi] is nearest (in log scale) to the batch's own: the 2nd..98th",
-           "// percentile of sqrt(n1*n2) over its pairs -- unless the caller set its own.",
+           "// beside the profiles).  A batch is planned with the entry whose range [lo, hi]",
+           "// is nearest (in log scale) to the batch's own -- both the 2nd..98th percentile",
+           "// of sqrt(n1*n2) + 1 over the pairs, for an entry those of the batch it was",
+           "// tuned on -- unless the caller set its own.",
            "#pragma once", "", "namespace gme {", "",
-           "struct TunedBucket {", "  int lo, hi;", "  int warps_per_block, blocks_per_sm;",
-           "  long long block_min_cells, team_min_cells;", "};", "",
+           "struct TunedBucket {", "  float lo, hi;", "  int warps_per_block, blocks_per_sm;",
+           "  long long block_min_cells, team_min_cells;", "  int team_split;", "};", "",
            f"constexpr int TUNED_BUCKETS = {len(keys)};",
            "constexpr TunedBucket TUNED[TUNED_BUCKETS > 0 ? TUNED_BUCKETS : 1] = {"]
-    for name, lo, hi in keys:
+    for bi, (name, lo, hi) in enumerate(BUCKETS + MIXES):
+        if name not in best:
+            continue
         r = best[name]
-        out.append(f"    {{{lo}, {hi}, {r['warps_per_block']}, {r['blocks_per_sm']}, {r['block_min_cells']}ll, "
-                   f"{r['team_min_cells']}ll}},  // {name}: {r['gcups']:.0f} GCUPS")
+        p_lo, p_hi = (r["p_lo"], r["p_hi"]) if "p_lo" in r else bucket_range(lo, hi, cells, 0x5EED + bi)
+        out.append(f"    {{{p_lo:.1f}f, {p_hi:.1f}f, {r['warps_per_block']}, {r['blocks_per_sm']}, {r['block_min_cells']}ll, "
+                   f"{r['team_min_cells']}ll, {r.get('team_split', 2)}}},  // {name}: {r['gcups']:.0f} GCUPS")
     if not keys:
-        out.append("    {0, 0, 4, 0, 1ll << 22, 1ll << 25},")
+        out.append("    {1.0f, 1.0f, 4, 0, 1ll << 22, 1ll << 25, 2},")
     out += ["};", "", "}  // namespace gme", ""]
     with open(path, "w") as f:
         f.write("\n".join(out))
@@ -280,7 +314,7 @@ def write_plain_md(rows, best, path, cmd):
              "up to the SM count.  Every shape's score equals the first shape's.", "",
              "| n | rows/lane | warps/band | grid | ms | GCUPS | |", "|---:|---:|---:|---:|---:|---:|---|"]
     for r in rows:
-        mark = "best" if best.get(r["n"]) is r else ("" if r["ok"] else "MISMATCH")
+        mark = "best" if best.get(r["n"]) == r else ("" if r["ok"] else "MISMATCH")
         lines.append(f"| {r['n']} | {r['rows_per_lane']} | {r['warps_per_band']} | {r['grid']} | "
                      f"{r['ms']:.3f} | {r['gcups']:.1f} | {mark} |")
     with open(path, "w") as f:
@@ -322,7 +356,7 @@ def main():
                  + f" --out-md {a.out_md}")
     if a.header:
         gen_header(best)
-    print(json.dumps({k: {"gcups": v["gcups"], **{kk: v[kk] for kk in GRID}} for k, v in best.items()}))
+    print(json.dumps({k: {"gcups": v["gcups"], **{kk: v.get(kk) for kk in GRID}} for k, v in best.items()}))
 
 
 if __name__ == "__main__":

@@ -146,7 +146,8 @@ typedef struct gme_batch_config {
   int32_t packed16;        /* 0 or 1: pairs whose scores provably fit 16 bits (and whose
                             * symbols lie in [0, 32767]) run two cells per register on s16x2
                             * DPX (the default); -1: int32 for every pair */
-  int32_t reserved;
+  int32_t team_split;      /* groups of bands per team member: a team job of G groups runs
+                            * on clamp(G / team_split, 2, 8) CTAs (0 = 2) */
 } gme_batch_config;
 
 gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg);

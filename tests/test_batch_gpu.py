@@ -76,10 +76,11 @@ def test_wide_pairs(gme_ctx, nw):
         gme_ctx.set_batch_config()
 
 
-@pytest.mark.parametrize("nw", [4, 8])
-def test_team_jobs(gme_ctx, nw):
+@pytest.mark.parametrize("nw,split", [(4, 2), (8, 2), (4, 3), (4, 1)])
+def test_team_jobs(gme_ctx, nw, split):
     """Pairs shared by teams of CTAs (every T-th band group per CTA, rows handed over
-    through global tagged rows); SW maxima with ties combined across the team."""
+    through global tagged rows, T = groups / split in 2..8); SW maxima with ties
+    combined across the team."""
     rng = np.random.default_rng(202 + nw)
     kinds, sa, sb = [], [], []
     for i in range(24):
@@ -104,7 +105,7 @@ def test_team_jobs(gme_ctx, nw):
         sa.append(rng.integers(0, 4, int(rng.integers(1, 3000))))
         sb.append(rng.integers(0, 4, int(rng.integers(1, 3000))))
     gme_ctx.set_batch_config(warps_per_block=nw, team_min_cells=1 << 18, long_min_cells=-1,
-                             block_min_cells=1 << 20, packed16=1 if nw == 4 else -1)
+                             block_min_cells=1 << 20, packed16=1 if nw == 4 else -1, team_split=split)
     try:
         for _ in range(2):
             check_batch(gme_ctx, kinds, sa, sb, rule=1)

@@ -85,6 +85,30 @@ def test_served_small_budget_many_waves():
     assert st["hbm_bytes_peak"] <= budget
 
 
+def test_served_queue_full_takes_prefix():
+    """A full queue takes a prefix of a submit_many call (its tickets are returned);
+    the rest submitted again later completes exactly like the rest."""
+    import time
+    import gpumemefficient_gb300 as g
+    rng = np.random.default_rng(13)
+    kinds, sa, sb = _requests(rng, 500, hi=2000)
+    symbols, pairs = g.pack_batch(kinds, sa, sb)
+    sc = g.scoring()
+    with g.Server(0, sc=sc, queue_max=64) as srv:
+        first = srv.submit_many(symbols, pairs)
+        assert 0 < len(first) <= 64
+        tickets = list(first)
+        rest = pairs[len(first):]
+        while len(rest):
+            t = srv.submit_many(symbols, rest)
+            tickets += list(t)
+            rest = rest[len(t):]
+            if len(rest):
+                time.sleep(0.001)
+        results = _collect(srv, tickets)
+    _check(results, kinds, sa, sb, sc, 0)
+
+
 def test_served_poll_single_and_threads():
     """gme_poll per ticket, two submitting threads, unknown tickets rejected."""
     import gpumemefficient_gb300 as g
