@@ -154,6 +154,8 @@ def run_reference(args):
         return
     if args.workload == "batched":
         return run_reference_batch(args, ws)
+    if args.workload == "sat":
+        return run_reference_sat(args, ws)
     kind, a, b, cfg = workload(args.workload)
     from oracle import oracle as O
     threads = os.cpu_count() or 1
@@ -175,6 +177,37 @@ def run_reference(args):
             "cpu_baseline": {"value": val, "unit": "GCUPS", "cores": threads, "kind": "port",
                              "sample": f"{KIND_NAME[kind]} {len(a)} columns x {rows} rows per step "
                                        f"({cells:.3g} cells), oracle/oracle.c on {threads} threads"},
+            "e2e": {"value": val, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_sat(args, ws):
+    """Reference arm, SAT workload: the recurrence on the CPU (oracle port, one thread: the
+    recurrence is sequential along each row) over a bounded band of rows per step."""
+    from oracle import oracle as O
+    n1 = args.sat_n
+    ld = n1 + 3
+    k = min(args.sat_n, 1024)
+    rng = np.random.default_rng(0x5A7)
+    host = rng.integers(0, 10000, (k + 1, ld), dtype=np.int32)
+    for _ in range(args.warmup):
+        O.lib().orc_sat(O._p32(host), n1, k, ld)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.lib().orc_sat(O._p32(host), n1, k, ld)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    val = n1 * k * len(times) / tot / 1e9
+    cfg = {"workload": f"summed-area table, {n1} x {n1} interior in the reference's layout, in place",
+           "n1": n1, "n2": n1, "ld": ld, "seed": 0x5A7}
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GCUPS",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32 (wrapping)",
+            "data": "synthetic (seeded)", "config": cfg,
+            "cpu_baseline": {"value": val, "unit": "GCUPS", "cores": 1, "kind": "port",
+                             "sample": f"rows 1..{k} of the table per step ({n1 * k:.3g} cells), "
+                                       "oracle/oracle.c on 1 thread"},
             "e2e": {"value": val, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -694,6 +727,107 @@ def run_gme_path(args):
     return line
 
 
+def run_gme_sat(args):
+    """Summed-area table of the reference's SAT case `15 15` (a 32768 x 32768 interior
+    in the reference's layout: n2 + 2 rows of n1 + 3 ints, values rand() % 10000 as its
+    generator writes them), in place on the device: cell updates per second, HBM
+    roofline at 8 bytes per cell (each cell read and written once)."""
+    import json as _json
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    import __graft_entry__ as ge
+    ge.build()
+    import gpumemefficient_gb300 as g
+    from oracle import oracle as O
+    n1 = n2 = args.sat_n
+    ld = n1 + 3
+    rng = np.random.default_rng(0x5A7)
+    host = rng.integers(0, 10000, (n2 + 2, ld), dtype=np.int32)
+    cells = n1 * n2
+    ctx = g.Context(local)
+    dev = torch.device("cuda", local)
+    # one explicit stream for the copies, the kernel and the events (a null stream
+    # handle would mean the library's own stream)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    d0 = torch.from_numpy(host).to(dev)
+    d = torch.empty_like(d0)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    # parity: the whole table against the oracle (outside the timed region)
+    d.copy_(d0)
+    ctx.sat_device(d.data_ptr(), n1, n2, ld, status.data_ptr(), stream.cuda_stream)
+    stream.synchronize()
+    got = d.cpu().numpy()
+    want = O.sat(host, n1, n2)
+    parity = bool(int(status.item()) == 0 and np.array_equal(got, want))
+    del got, want
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(args.warmup):
+        d.copy_(d0)
+        ctx.sat_device(d.data_ptr(), n1, n2, ld, status.data_ptr(), stream.cuda_stream)
+    times = []
+    l0 = ctx.launches
+    clocks = ClockSampler(local)
+    for _ in range(args.steps):
+        d.copy_(d0)          # the input back (untimed); then L2 emptied of it
+        flush.fill_(1)
+        e0.record(stream)
+        ctx.sat_device(d.data_ptr(), n1, n2, ld, status.data_ptr(), stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    clk = clocks.stop()
+    launches = ctx.launches - l0
+    ok_status = int(status.item()) == 0
+    t = sum(times) / len(times)
+    value = cells / t / 1e9
+    # end to end through gme_sat: pinned host table in, rows 1..n2 back, every step
+    pinned = torch.from_numpy(host).pin_memory()
+    ctx.sat(pinned.numpy(), n1, n2)
+    et = []
+    for _ in range(max(1, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        ctx.sat(pinned.numpy(), n1, n2)  # in place: each step recomputes on the last output (same work)
+        et.append(time.perf_counter() - t0)
+    e2e = cells / (sum(et) / len(et)) / 1e9
+    try:
+        peak = _json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))["hbm_gbs"]
+        basis = "MEASURED_PEAKS.json hbm_gbs (copy, measured on this pool)"
+    except (OSError, KeyError, ValueError):
+        peak, basis = 6800.0, "fallback 6.8 TB/s"
+    achieved = 8.0 * cells / t / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": profiled_traffic("sat_kernel_32768"), "peak_basis": basis,
+            "bytes_per_cell": 8, "kernel": "sat_kernel (one launch)"}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        k = 2048
+        sample = host[:k + 1].copy()
+        t0 = time.perf_counter()
+        O.lib().orc_sat(O._p32(sample), n1, k, ld)
+        dt = time.perf_counter() - t0
+        cpu = {"value": n1 * k / dt / 1e9, "unit": "GCUPS", "cores": 1, "kind": "port",
+               "sample": f"rows 1..{k} of the table ({n1 * k:.3g} cells), oracle/oracle.c on 1 thread, {dt:.2f} s"}
+    cfg = {"workload": f"summed-area table, {n1} x {n2} interior in the reference's layout "
+                       f"({n2 + 2} rows of {ld} ints, values 0..9999 seeded), in place, one launch",
+           "n1": n1, "n2": n2, "ld": ld, "seed": 0x5A7,
+           "l2": "table (4.3 GB at 32768) larger than L2; input restored and L2 flushed (256 MiB write) before each step",
+           "parity_vs_oracle": "ok" if parity and ok_status else "MISMATCH"}
+    line = {"metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32 (wrapping)", "data": "synthetic (seeded)", "config": cfg,
+            "clocks": clk,
+            "e2e": {"value": e2e, "unit": "GCUPS", "h2d_bytes_per_step": int((n2 + 1) * ld * 4),
+                    "d2h_bytes_per_step": int(n2 * ld * 4), "note": "gme_sat from pinned host memory"},
+            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
+            "step_ms": {"min": 1e3 * min(times), "median": 1e3 * statistics.median(times),
+                        "max": 1e3 * max(times)}}
+    ctx.close()
+    return line
+
+
 def _walk(ops):
     i = j = 0
     for c in ops:
@@ -729,6 +863,8 @@ def main():
     p.add_argument("--rate-seconds", type=float, default=2.0, help="served workload: seconds per rate point")
     p.add_argument("--wave-cells", type=int, default=0, help="served workload: cells per launch at most (0 = default)")
     p.add_argument("--no-parity", action="store_true", help="skip the oracle parity check (tuning runs)")
+    p.add_argument("--sat-n", type=int, default=32768,
+                   help="sat workload: interior side (the reference's `15 15` case is 32768)")
     p.add_argument("--solo", action="store_true",
                    help="default workload only (no batched/served summaries beside it)")
     args = p.parse_args()
@@ -743,6 +879,8 @@ def main():
         line = run_gme_served(args)
     elif args.workload == "path":
         line = run_gme_path(args)
+    elif args.workload == "sat":
+        line = run_gme_sat(args)
     else:
         line = run_gme(args)
         ws = dist_env()[0]

@@ -128,6 +128,8 @@ def _declare(L):
     L.gme_server_get_stats.argtypes = [_vp, c.POINTER(ServerStats)]
     L.gme_server_last_error.argtypes = [_vp]
     L.gme_server_last_error.restype = c.c_char_p
+    L.gme_sat_device.argtypes = [_vp, _vp, c.c_int64, c.c_int64, c.c_int64, _vp, _vp]
+    L.gme_sat.argtypes = [_vp, _vp, c.c_int64, c.c_int64, c.c_int64]
     L.gme_align_path.argtypes = [_vp, c.c_int, _vp, c.c_int64, _vp, c.c_int64, c.POINTER(Scoring), _vp,
                                  c.c_int64, c.POINTER(c.c_int64), c.POINTER(c.c_int32)]
     L.gme_debug_wait_timeout.argtypes = [_vp, c.c_uint64, c.POINTER(c.c_int32)]
@@ -302,6 +304,21 @@ class Context:
                                     ctypes.byref(scoring_), buf, cap, ctypes.byref(n), ctypes.byref(sc_)),
                self.handle)
         return sc_.value, buf.raw[:n.value].decode()
+
+    def sat(self, table, n1: int, n2: int) -> np.ndarray:
+        """Summed-area table (``gme_sat``) of a host int32 table of rows 0..n2 (row length
+        >= n1 + 1; the reference's layout has n1 + 3): rows 1..n2 x columns 1..n1 are
+        rewritten in place; returns the table."""
+        t = table if isinstance(table, np.ndarray) and table.dtype == np.int32 and \
+            table.flags.c_contiguous else np.ascontiguousarray(table, dtype=np.int32)
+        assert t.ndim == 2 and t.shape[0] >= n2 + 1 and t.shape[1] >= n1 + 1
+        _check(lib().gme_sat(self.handle, t.ctypes.data, n1, n2, t.shape[1]), self.handle)
+        return t
+
+    def sat_device(self, d_table: int, n1: int, n2: int, ld: int, d_status: int = 0, stream: int = 0):
+        """``gme_sat_device``: in place on a device table, asynchronous on ``stream``."""
+        _check(lib().gme_sat_device(self.handle, d_table, n1, n2, ld, d_status or None, stream or None),
+               self.handle)
 
     def debug_wait_timeout(self, timeout_ns: int) -> int:
         """Runs a bounded device wait on a flag nothing sets; returns the kernel's status."""

@@ -185,6 +185,8 @@ struct gme_context {
   gme::BatchTuning batch_tune;
   int *d_bsym = nullptr; long long d_bsym_cap = 0;
   gme_result *d_bres = nullptr; long long d_bres_cap = 0;
+  // summed-area table staging for the host-buffer entry point
+  int *d_sat = nullptr; long long d_sat_cap = 0;
 };
 
 using gme::ST_OK;
@@ -311,7 +313,7 @@ gme_status gme_destroy(gme_context *ctx) {
   cudaStreamSynchronize(ctx->stream);
   ctx->ws.release();
   ctx->batch.release();
-  cudaFree(ctx->d_bsym); cudaFree(ctx->d_bres);
+  cudaFree(ctx->d_bsym); cudaFree(ctx->d_bres); cudaFree(ctx->d_sat);
   cudaFree(ctx->d_a); cudaFree(ctx->d_b); cudaFree(ctx->d_row); cudaFree(ctx->d_col);
   cudaFree(ctx->d_res);
   cudaFreeHost(ctx->h_res);
@@ -411,6 +413,38 @@ gme_status gme_align(gme_context *ctx, gme_kind kind, const int32_t *a, int64_t 
   if (out->status != 0) {
     ctx->ws.last_error = "device-side wait timed out";
     return to_status(out->status);
+  }
+  return GME_OK;
+}
+
+gme_status gme_sat_device(gme_context *ctx, int32_t *d_table, int64_t n1, int64_t n2, int64_t ld,
+                          int32_t *d_status, void *stream) {
+  if (!ctx || (n1 > 0 && n2 > 0 && !d_table)) return GME_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  return to_status(gme::sat_run(ctx->ws, d_table, n1, n2, ld, d_status, st, ctx->timeout_ns));
+}
+
+gme_status gme_sat(gme_context *ctx, int32_t *table, int64_t n1, int64_t n2, int64_t ld) {
+  if (!ctx || n1 < 0 || n2 < 0 || ld < n1 + 1 || (n1 > 0 && n2 > 0 && !table)) return GME_ERR_INVALID;
+  if (n1 == 0 || n2 == 0) return GME_OK;
+  cudaSetDevice(ctx->device);
+  const long long cells = (n2 + 1) * ld;
+  int rc;
+  if ((rc = grow_dev((void **)&ctx->d_sat, &ctx->d_sat_cap, cells, 4, ctx))) return to_status(rc);
+  cudaStream_t st = ctx->stream;
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(ctx->d_sat, table, (size_t)cells * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return to_status(ctx->ws.fail(e, "cudaMemcpyAsync(sat table)"));
+  gme_status s = to_status(gme::sat_run(ctx->ws, ctx->d_sat, n1, n2, ld, &ctx->d_res->status, st, ctx->timeout_ns));
+  if (s != GME_OK) return s;
+  if ((e = cudaMemcpyAsync(table + ld, ctx->d_sat + ld, (size_t)(cells - ld) * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(ctx->h_res, ctx->d_res, sizeof(gme_result), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return to_status(ctx->ws.fail(e, "cudaMemcpyAsync(sat result)"));
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return to_status(ctx->ws.fail(e, "cudaStreamSynchronize"));
+  if (ctx->h_res->status != 0) {
+    ctx->ws.last_error = "sat: device-side wait timed out";
+    return to_status(ctx->h_res->status);
   }
   return GME_OK;
 }

@@ -116,6 +116,10 @@ constexpr int BATCH_MAX_N1 = 16384;  // widest pair the batch kernel takes (wide
 long long batch_pair_bytes(long long n1, long long n2);
 long long batch_grid(int sms, int NW, int blocks_per_sm);
 long long batch_scratch_bytes(long long grid, int NW, int max_n1);
+// summed-area table (gme_sat.cu)
+int sat_run(Workspace &ws, int *d_table, long long n1, long long n2, long long ld, int *d_status,
+            cudaStream_t st, unsigned long long timeout_ns);
+long long sat_scratch_words(long long n1, long long n2);
 int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long npairs,
                long long nsym, const BatchTuning &tune, cudaStream_t st,
                const long long *row_offs = nullptr, const long long *col_offs = nullptr);

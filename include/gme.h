@@ -273,6 +273,23 @@ gme_status gme_align_path(gme_context *ctx, gme_kind kind, const int32_t *a, int
                           const int32_t *b, int64_t n2, const gme_scoring *sc, char *ops,
                           int64_t ops_cap, int64_t *n_ops, int32_t *score);
 
+/* ---- summed-area table (SAT/GPU_Hyperlane_Share.cu) -----------------------------
+ * In place on an int32 table of rows 0..n2 with row stride ld (>= n1 + 1; the
+ * reference's layout has ld = n1 + 3): every cell of rows 1..n2 and columns 1..n1
+ * becomes t[y][x-1] + t[y-1][x] + t[y][x] - t[y-1][x-1] (the reference's recurrence,
+ * SAT/GPU_Hyperlane_Share.cu:169,196,231), evaluated row after row, left to right,
+ * in wrapping 32-bit arithmetic; row 0 and column 0 keep their values, columns
+ * beyond n1 are not touched.  One launch over column strips, rows handed from strip
+ * to strip as tagged words with bounded waits.
+ * gme_sat_device: device table, asynchronous on `stream`; d_status (may be NULL)
+ * receives 0 or GME_ERR_TIMEOUT when the kernel has run.  gme_sat: host table (rows
+ * 0..n2 copied in and rows 1..n2 back), blocking.  Replaces the reference's
+ * SOR(n1, n2, table, tX, tY) (SAT/GPU_Hyperlane_Share.h:5), which computes the same
+ * table on the device but never copies it back. */
+gme_status gme_sat_device(gme_context *ctx, int32_t *d_table, int64_t n1, int64_t n2, int64_t ld,
+                          int32_t *d_status, void *stream);
+gme_status gme_sat(gme_context *ctx, int32_t *table, int64_t n1, int64_t n2, int64_t ld);
+
 /* ---- plain path without allocation --------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc (code
  * running inside another runtime's memory pool, a plugin that must not allocate on

@@ -47,6 +47,12 @@ int SW(int n1, int n2, int *arr1, int *arr2, int paddX, int paddY, int *table, i
 int SW(int n1, int n2, int *arr1, int *arr2, int paddX, int paddY, int *table);
 /* SmithWaterman/GPU.h:5 */
 int SW(int n1, int n2, int *arr1, int *arr2);
+/* SAT/GPU_Hyperlane_Share.h:5, SAT/GPU_Hyperlane_Cache.h:5: the summed-area table of
+ * the reference's layout (rows 0..n2, row length n1 + 3; gme_sat).  Unlike the
+ * reference, which leaves `table` untouched (its copy back is commented out,
+ * SAT/GPU_Hyperlane_Share.cu:321), rows 1..n2 x columns 1..n1 of `table` receive
+ * the result.  tX, tY are accepted and ignored. */
+void SOR(int n1, int n2, int *table, int tX, int tY);
 #endif
 
 #ifdef __cplusplus
@@ -58,6 +64,8 @@ gme_status gme_reference_last_status(void);
 int32_t gme_ref_lcs(int32_t n1, int32_t n2, const int32_t *arr1, const int32_t *arr2);
 int32_t gme_ref_ed(int32_t n1, int32_t n2, const int32_t *arr1, const int32_t *arr2);
 int32_t gme_ref_sw(int32_t n1, int32_t n2, const int32_t *arr1, const int32_t *arr2);
+/* SOR for FFI users: 0 on success, else the gme_status. */
+int32_t gme_ref_sor(int32_t n1, int32_t n2, int32_t *table);
 #ifdef __cplusplus
 }
 #endif

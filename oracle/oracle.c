@@ -311,3 +311,23 @@ void orc_align_batch_mt(const int32_t *kinds, const int32_t *seq,
     for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
     free(th);
 }
+
+/*
+ * Summed-area table, in place: the recurrence of the reference's SAT kernels,
+ *   t[y][x] = t[y][x-1] + t[y-1][x] + t[y][x] - t[y-1][x-1]
+ * (SAT/GPU_Hyperlane_Share.cu:169 first tiles, :231 last tiles; the same
+ * expression at :196 for the hyperlane tiles), over rows 1..n2 and columns 1..n1
+ * of a table with row stride ld (the reference's host function allocates rows of
+ * n1 + 3 ints, SAT/GPU_Hyperlane_Share.cu:245-248, and its tiles start at row 1,
+ * column 1 and end at column n1, :155-162, :210-214).  Row 0 and column 0 keep their
+ * values.  Evaluated row after row, left to right, in 32-bit unsigned arithmetic
+ * (the int wrap-around of the GPU).
+ */
+void orc_sat(int32_t *t, int64_t n1, int64_t n2, int64_t ld) {
+    for (int64_t y = 1; y <= n2; ++y) {
+        uint32_t *row = (uint32_t *)t + y * ld;
+        const uint32_t *up = (const uint32_t *)t + (y - 1) * ld;
+        for (int64_t x = 1; x <= n1; ++x)
+            row[x] = row[x - 1] + up[x] + row[x] - up[x - 1];
+    }
+}

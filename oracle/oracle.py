@@ -67,6 +67,8 @@ def lib():
                                              ctypes.c_int64, ctypes.c_int, ctypes.c_int32,
                                              ctypes.c_int32, ctypes.c_int32, _i32p, _i32p, _i64p,
                                              _i64p, ctypes.c_int]
+            L.orc_sat.restype = None
+            L.orc_sat.argtypes = [_i32p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]
             _lib = L
     return _lib
 
@@ -167,3 +169,28 @@ def table_py(kind: int, a, b, rule: int = ED_REF_CPU, match: int = SW_MATCH,
                 v = max(left + gap, max(up + gap, max(diag + (match if eq else mismatch), 0)))
             t[y][x] = v
     return t
+
+
+def sat(table, n1: int, n2: int):
+    """Summed-area table of the reference's layout (rows 0..n2 of any row length
+    >= n1 + 1), returned as a new int32 array: rows 1..n2 x columns 1..n1 follow the
+    SAT recurrence (SAT/GPU_Hyperlane_Share.cu:169,196,231) in wrapping 32-bit
+    arithmetic; everything else is copied."""
+    t = np.ascontiguousarray(table, dtype=np.int32).copy()
+    assert t.ndim == 2 and t.shape[0] >= n2 + 1 and t.shape[1] >= n1 + 1
+    lib().orc_sat(_p32(t), n1, n2, t.shape[1])
+    return t
+
+
+def sat_py(table, n1: int, n2: int):
+    """Independent restatement for cross-checks: the closed form of the recurrence,
+    t[y][x] = A[y][0] + A[0][x] - A[0][0] + sum_{1<=i<=y, 1<=j<=x} A[i][j] (mod 2^32),
+    with numpy cumulative sums."""
+    a = np.asarray(table, dtype=np.int64)
+    out = np.array(table, dtype=np.int32, copy=True)
+    if n1 == 0 or n2 == 0:
+        return out
+    inner = a[1:n2 + 1, 1:n1 + 1].cumsum(0).cumsum(1)
+    v = inner + a[1:n2 + 1, 0:1] + a[0:1, 1:n1 + 1] - a[0, 0]
+    out[1:n2 + 1, 1:n1 + 1] = (v & 0xffffffff).astype(np.uint32).view(np.int32)
+    return out
