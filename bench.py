@@ -799,7 +799,7 @@ def run_gme_sat(args):
         peak, basis = 6800.0, "fallback 6.8 TB/s"
     achieved = 8.0 * cells / t / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": profiled_traffic("sat_kernel_32768"), "peak_basis": basis,
+            "traffic": profiled_traffic("sat_kernel_16384"), "peak_basis": basis,
             "bytes_per_cell": 8, "kernel": "sat_kernel (one launch)"}
     cpu = None
     if rank == 0 and not args.no_cpu:
