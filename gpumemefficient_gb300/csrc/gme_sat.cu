@@ -48,13 +48,19 @@ namespace {
 constexpr int SAT_W = GME_SAT_WIDTH;         // strip width: one column per thread (64 or 128)
 constexpr int SAT_THREADS = SAT_W;
 constexpr int SAT_SEG = SAT_W / 32;          // 32-column segments per row
-constexpr int SAT_RB = SAT_THREADS / SAT_SEG;  // rows per block: 32
+#ifndef GME_SAT_ROWS
+#define GME_SAT_ROWS 32
+#endif
+// rows per block (measured at 32768 x 32768: 64 rows with 2 or 3 stages 2.82-2.84 ms
+// against 2.57 ms for 32 rows with 5)
+constexpr int SAT_RB = GME_SAT_ROWS;
+constexpr int SAT_RPT = SAT_RB / (SAT_THREADS / SAT_SEG);  // rows per row-scan lane group
 // blocks in shared memory (measured at 32768 x 32768: 3 stages 2.76 ms, 5 stages
 // 2.58 ms; 64-column strips 2.94-2.95 ms, their carries double)
 constexpr int SAT_STAGES = GME_SAT_STAGES;
 constexpr int SAT_PITCH = SAT_W + SAT_W / 32;  // a pad word per 32 columns
 static_assert(SAT_W == 64 || SAT_W == 128, "strip width 64 or 128");
-static_assert(SAT_RB == 32, "one row per lane group");
+static_assert(SAT_RB == 32 || SAT_RB == 64, "32 or 64 rows per block");
 constexpr unsigned FULL = 0xffffffffu;
 
 struct SatParams {
@@ -129,49 +135,68 @@ __global__ void __launch_bounds__(SAT_THREADS) sat_kernel(SatParams P) {
       issue(b + SAT_STAGES - 1);
       int *tile = sat_smem + (int)(b % SAT_STAGES) * (SAT_RB * SAT_PITCH);
       const long long y0 = 1 + b * SAT_RB;
-      // 2. row rr, segment g: serial prefix, then the four segments combined
-      int *rowp = tile + rr * SAT_PITCH + 33 * g;
-      unsigned pv[32];
-      unsigned acc = 0;
+      // 2. rows rr + 32q, segment g: serial prefix, then the row's segments combined
+      unsigned pv[SAT_RPT][32], inc[SAT_RPT], seg_excl[SAT_RPT], c[SAT_RPT];
+      bool live[SAT_RPT], done[SAT_RPT];
+      long long yq[SAT_RPT], jq[SAT_RPT];
 #pragma unroll
-      for (int i = 0; i < 32; ++i) { acc += (unsigned)rowp[i]; pv[i] = acc; }
-      unsigned inc = acc;
+      for (int q = 0; q < SAT_RPT; ++q) {
+        const int *rowp = tile + (rr + 32 * q) * SAT_PITCH + 33 * g;
+        unsigned acc = 0;
 #pragma unroll
-      for (int d = 1; d < SAT_SEG; d <<= 1) {
-        const unsigned t = __shfl_up_sync(FULL, inc, d, SAT_SEG);
-        if (g >= d) inc += t;
+        for (int i = 0; i < 32; ++i) { acc += (unsigned)rowp[i]; pv[q][i] = acc; }
+        unsigned t = acc;
+#pragma unroll
+        for (int d = 1; d < SAT_SEG; d <<= 1) {
+          const unsigned u = __shfl_up_sync(FULL, t, d, SAT_SEG);
+          if (g >= d) t += u;
+        }
+        inc[q] = t;
+        seg_excl[q] = t - acc;
+        // the row's last segment holds the row total (rows beyond n2 and the other
+        // lanes read nothing and always agree)
+        yq[q] = y0 + rr + 32 * q;
+        live[q] = g == SAT_SEG - 1 && yq[q] <= n2;
+        c[q] = 0;
+        done[q] = !live[q];
+        jq[q] = s - 1;
+        if (s == 0) {
+          if (live[q]) c[q] = (unsigned)P.table[yq[q] * ld] - (unsigned)P.table[(yq[q] - 1) * ld];
+        } else if (live[q] && publish) {
+          st_relaxed_gpu_u64(own + yq[q], ((unsigned long long)tagw << 32) | inc[q]);
+        }
       }
-      const unsigned seg_excl = inc - acc;
-      // the row's last segment holds the row total: publish, look back, publish (rows
-      // beyond n2 and the other lanes read nothing and always agree)
-      const long long y = y0 + rr;
-      const bool live = g == SAT_SEG - 1 && y <= n2;
-      unsigned c = 0;
-      if (s == 0) {
-        if (live) c = (unsigned)P.table[y * ld] - (unsigned)P.table[(y - 1) * ld];
-      } else {
-        if (live && publish) st_relaxed_gpu_u64(own + y, ((unsigned long long)tagw << 32) | inc);
-        bool done = !live;
-        long long j = s - 1;
+      // look back for every row of this lane at once
+      if (s > 0) {
         const bool ok = W.wait([&] {
-          if (!done) {
-            const unsigned long long wv = ld_relaxed_gpu_u64(P.carry + j * P.cstride + y);
-            const unsigned hi = (unsigned)(wv >> 32);
-            if ((hi & ~1u) == tagw) {
-              c += (unsigned)wv;
-              if (hi & 1u) done = true;
-              else --j;  // an aggregate: strip j's own total; keep looking left
+#pragma unroll
+          for (int q = 0; q < SAT_RPT; ++q) {
+            if (!done[q]) {
+              const unsigned long long wv = ld_relaxed_gpu_u64(P.carry + jq[q] * P.cstride + yq[q]);
+              const unsigned hi = (unsigned)(wv >> 32);
+              if ((hi & ~1u) == tagw) {
+                c[q] += (unsigned)wv;
+                if (hi & 1u) done[q] = true;
+                else --jq[q];  // an aggregate: strip j's own total; keep looking left
+              }
             }
           }
-          return __all_sync(FULL, done);
+          bool all = true;
+#pragma unroll
+          for (int q = 0; q < SAT_RPT; ++q) all = all && done[q];
+          return __all_sync(FULL, all);
         });
         if (!ok) failed = true;
       }
-      if (live && publish && !failed)
-        st_relaxed_gpu_u64(own + y, ((unsigned long long)(tagw | 1u) << 32) | (c + inc));
-      const unsigned off = __shfl_sync(FULL, c, (lane & ~(SAT_SEG - 1)) | (SAT_SEG - 1)) + seg_excl;
 #pragma unroll
-      for (int i = 0; i < 32; ++i) rowp[i] = (int)(pv[i] + off);
+      for (int q = 0; q < SAT_RPT; ++q) {
+        if (live[q] && publish && !failed)
+          st_relaxed_gpu_u64(own + yq[q], ((unsigned long long)(tagw | 1u) << 32) | (c[q] + inc[q]));
+        const unsigned off = __shfl_sync(FULL, c[q], (lane & ~(SAT_SEG - 1)) | (SAT_SEG - 1)) + seg_excl[q];
+        int *rowp = tile + (rr + 32 * q) * SAT_PITCH + 33 * g;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) rowp[i] = (int)(pv[q][i] + off);
+      }
       __syncthreads();  // (2) D_y(x) in place
       if (s_abort) break;
       // 3. column pass: t[y][x] = t[y-1][x] + D_y(x)
