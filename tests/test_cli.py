@@ -66,3 +66,37 @@ def test_align_cli_errors_without_data(tmp_path):
     assert r.returncode == 1
     r = subprocess.run([exe, "ED", "12"], capture_output=True, text=True)
     assert r.returncode == 1 and "Incorrect Input Parameters" in r.stdout
+
+
+def read_sat_text(path):
+    lines = open(path).read().split("\n")
+    n1, n2 = map(int, lines[0].split())
+    rows = [np.array(l.split(), np.int64) for l in lines[1:1 + n2 + 3]]
+    assert all(len(r) == n1 + 3 for r in rows) and lines[1].endswith(" ")
+    return n1, n2, np.stack(rows)
+
+
+def test_generate_sat_layout_and_seed(tmp_path):
+    """gme-generate --sat: the layout of SAT/generator.cpp (header, n2 + 3 rows of n1 + 3
+    values in 0..9999); smaller files hold the first values of the same array."""
+    gen = _tools()["gme-generate"]
+    for d in ("a", "b"):
+        (tmp_path / d).mkdir()
+        r = subprocess.run([gen, "--sat", "8", "7", "--min", "6", "--seed", "5", "--dir", str(tmp_path / d)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout
+    names = sorted(p.name for p in (tmp_path / "a").iterdir())
+    assert names == ["x_2_6_y_2_5.txt", "x_2_7_y_2_6.txt", "x_2_8_y_2_7.txt"]
+    for nm in names:
+        assert (tmp_path / "a" / nm).read_bytes() == (tmp_path / "b" / nm).read_bytes()
+    n1, n2, big = read_sat_text(tmp_path / "a" / "x_2_8_y_2_7.txt")
+    assert (n1, n2) == (256, 128) and big.min() >= 0 and big.max() <= 9999
+    s1, s2, small = read_sat_text(tmp_path / "a" / "x_2_7_y_2_6.txt")
+    flat = big.reshape(-1)
+    np.testing.assert_array_equal(small.reshape(-1), flat[:(s1 + 3) * (s2 + 3)])
+
+
+def test_align_sat_missing_file_fails(tmp_path):
+    r = subprocess.run([_tools()["gme-align"], "SAT", "9", "9", "32", "128", "1", "--dir", str(tmp_path)],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "cannot be opened" in r.stdout

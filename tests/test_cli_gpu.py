@@ -59,3 +59,23 @@ def test_generated_data_end_to_end(tmp_path):
     b = np.array(lines[2].split(), np.int32)
     out = run(["ED", "9", "8", "--border", "gpu"], tmp_path)
     assert out[0] == f"last: {O.align(1, a, b, rule=O.ED_STANDARD)['score']}"
+
+
+def test_sat_driver_matches_oracle(tmp_path):
+    """gme-align SAT E1 E2 TX TY ITR on a generated file: the reference driver's output
+    line, and with --out the table equal to the oracle's."""
+    from test_cli import read_sat_text
+    tools = _tools()
+    r = subprocess.run([tools["gme-generate"], "--sat", "9", "8", "--min", "9", "--seed", "7", "--dir",
+                        str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+    out = tmp_path / "out.txt"
+    r = subprocess.run([tools["gme-align"], "SAT", "9", "8", "16", "64", "3", "--dir", str(tmp_path),
+                        "--out", str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = r.stdout.splitlines()
+    assert len(lines) == 1 and lines[0].startswith("execution time: ") and lines[0].endswith(" ms.")
+    n1, n2, t_in = read_sat_text(tmp_path / "x_2_9_y_2_8.txt")
+    _, _, t_out = read_sat_text(out)
+    want = O.sat(t_in.astype(np.int32), n1, n2)
+    np.testing.assert_array_equal(t_out, want.astype(np.int64))
