@@ -128,6 +128,7 @@ def _declare(L):
     L.gme_server_get_stats.argtypes = [_vp, c.POINTER(ServerStats)]
     L.gme_server_last_error.argtypes = [_vp]
     L.gme_server_last_error.restype = c.c_char_p
+    L.gme_batch_tuned_config.argtypes = [_vp, c.c_int64, c.POINTER(BatchConfig)]
     L.gme_sat_device.argtypes = [_vp, _vp, c.c_int64, c.c_int64, c.c_int64, _vp, _vp]
     L.gme_sat.argtypes = [_vp, _vp, c.c_int64, c.c_int64, c.c_int64]
     L.gme_align_path.argtypes = [_vp, c.c_int, _vp, c.c_int64, _vp, c.c_int64, c.POINTER(Scoring), _vp,
@@ -454,6 +455,15 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def batch_tuned_config(pairs: np.ndarray) -> dict:
+    """The autotuned settings a batch of these pairs (PAIR_DTYPE; only n1, n2 matter) is
+    planned with when no configuration is set (``gme_batch_tuned_config``; no GPU needed)."""
+    pairs = np.ascontiguousarray(pairs, PAIR_DTYPE)
+    cfg = BatchConfig()
+    _check(lib().gme_batch_tuned_config(pairs.ctypes.data, len(pairs), ctypes.byref(cfg)))
+    return {n: getattr(cfg, n) for n, _ in BatchConfig._fields_}
 
 
 def pack_batch(kinds, seqs_a, seqs_b):

@@ -417,6 +417,19 @@ gme_status gme_align(gme_context *ctx, gme_kind kind, const int32_t *a, int64_t 
   return GME_OK;
 }
 
+gme_status gme_batch_tuned_config(const gme_pair *pairs, int64_t n, gme_batch_config *out) {
+  if (!out || n < 0 || (n > 0 && !pairs)) return GME_ERR_INVALID;
+  const gme::BatchTuning t = gme::batch_tuning_for(pairs, n, gme::BatchTuning{});
+  out->warps_per_block = t.warps_per_block;
+  out->blocks_per_sm = t.blocks_per_sm;
+  out->block_min_cells = t.block_min_cells;
+  out->long_min_cells = 0;
+  out->team_min_cells = t.team_min_cells;
+  out->packed16 = 0;
+  out->team_split = t.team_split;
+  return GME_OK;
+}
+
 gme_status gme_sat_device(gme_context *ctx, int32_t *d_table, int64_t n1, int64_t n2, int64_t ld,
                           int32_t *d_status, void *stream) {
   if (!ctx || (n1 > 0 && n2 > 0 && !d_table)) return GME_ERR_INVALID;

@@ -116,6 +116,8 @@ constexpr int BATCH_MAX_N1 = 16384;  // widest pair the batch kernel takes (wide
 long long batch_pair_bytes(long long n1, long long n2);
 long long batch_grid(int sms, int NW, int blocks_per_sm);
 long long batch_scratch_bytes(long long grid, int NW, int max_n1);
+// the tuned table's entry for a batch of pairs (given.user_set: `given` itself)
+BatchTuning batch_tuning_for(const gme_pair *pairs, long long npairs, const BatchTuning &given);
 // summed-area table (gme_sat.cu)
 int sat_run(Workspace &ws, int *d_table, long long n1, long long n2, long long ld, int *d_status,
             cudaStream_t st, unsigned long long timeout_ns);

@@ -151,6 +151,11 @@ typedef struct gme_batch_config {
 } gme_batch_config;
 
 gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg);
+/* The settings a batch of these pairs is planned with when no configuration was set:
+ * the entry of the autotuned table whose length range (2nd..98th percentile of
+ * sqrt(n1*n2)) is nearest the batch's, in log scale.  Host only, needs no GPU.
+ * long_min_cells is 0 (automatic) and packed16 is 0 (on) in the result. */
+gme_status gme_batch_tuned_config(const gme_pair *pairs, int64_t n, gme_batch_config *out);
 /* Host buffers; blocks until all results are in `results`. */
 gme_status gme_align_batch(gme_context *ctx, const int32_t *symbols, int64_t nsym,
                            const gme_pair *pairs, int64_t npairs, const gme_scoring *sc,
