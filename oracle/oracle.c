@@ -331,3 +331,61 @@ void orc_sat(int32_t *t, int64_t n1, int64_t n2, int64_t ld) {
             row[x] = row[x - 1] + up[x] + row[x] - up[x - 1];
     }
 }
+
+/*
+ * The same table with all host threads, for the CPU baselines: the recurrence above
+ * telescopes to t[y][x] = A[y][0] + A[0][x] - A[0][0] + sum_{1<=i<=y, 1<=j<=x} A[i][j]
+ * (mod 2^32), so pass 1 turns each row into its prefix sums (rows across threads) and
+ * pass 2 accumulates them down each column and adds the borders (column blocks across
+ * threads).  Equal to orc_sat bit for bit; tested against it.
+ */
+typedef struct {
+    uint32_t *t;
+    int64_t n1, n2, ld;
+    int pass, nthreads, id;
+} sat_arg;
+
+static void *sat_worker(void *p) {
+    sat_arg *g = (sat_arg *)p;
+    if (g->pass == 1) {
+        for (int64_t y = 1 + g->id; y <= g->n2; y += g->nthreads) {
+            uint32_t *row = g->t + y * g->ld, acc = 0;
+            for (int64_t x = 1; x <= g->n1; ++x) { acc += row[x]; row[x] = acc; }
+        }
+    } else {
+        const int64_t blk = 1024;
+        const uint32_t *top = g->t;
+        for (int64_t x0 = 1 + g->id * blk; x0 <= g->n1; x0 += g->nthreads * blk) {
+            const int64_t x1 = x0 + blk - 1 < g->n1 ? x0 + blk - 1 : g->n1;
+            for (int64_t y = 1; y <= g->n2; ++y) {
+                uint32_t *row = g->t + y * g->ld;
+                const uint32_t *up = g->t + (y - 1) * g->ld;
+                const uint32_t left = row[0] - top[0];  /* A[y][0] - A[0][0] */
+                if (y == 1) {
+                    for (int64_t x = x0; x <= x1; ++x) row[x] = top[x] + left + row[x];
+                } else {
+                    const uint32_t upleft = up[0] - top[0];  /* A[y-1][0] - A[0][0] */
+                    for (int64_t x = x0; x <= x1; ++x) row[x] = up[x] - upleft + left + row[x];
+                }
+            }
+        }
+    }
+    return NULL;
+}
+
+void orc_sat_mt(int32_t *t, int64_t n1, int64_t n2, int64_t ld, int nthreads) {
+    if (n1 <= 0 || n2 <= 0) return;
+    if (nthreads < 1) nthreads = 1;
+    pthread_t *th = (pthread_t *)malloc((size_t)nthreads * sizeof(pthread_t));
+    sat_arg *args = (sat_arg *)malloc((size_t)nthreads * sizeof(sat_arg));
+    for (int pass = 1; pass <= 2; ++pass) {
+        for (int i = 0; i < nthreads; ++i) {
+            sat_arg a = {(uint32_t *)t, n1, n2, ld, pass, nthreads, i};
+            args[i] = a;
+            pthread_create(&th[i], NULL, sat_worker, &args[i]);
+        }
+        for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    }
+    free(th);
+    free(args);
+}

@@ -69,6 +69,8 @@ def lib():
                                              _i64p, ctypes.c_int]
             L.orc_sat.restype = None
             L.orc_sat.argtypes = [_i32p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]
+            L.orc_sat_mt.restype = None
+            L.orc_sat_mt.argtypes = [_i32p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int]
             _lib = L
     return _lib
 
@@ -179,6 +181,15 @@ def sat(table, n1: int, n2: int):
     t = np.ascontiguousarray(table, dtype=np.int32).copy()
     assert t.ndim == 2 and t.shape[0] >= n2 + 1 and t.shape[1] >= n1 + 1
     lib().orc_sat(_p32(t), n1, n2, t.shape[1])
+    return t
+
+
+def sat_mt(table, n1: int, n2: int, threads: int = 0):
+    """``sat`` on all host threads (row prefixes, then column accumulation; the CPU
+    baselines' form), bit-identical to ``sat``."""
+    t = np.ascontiguousarray(table, dtype=np.int32).copy()
+    assert t.ndim == 2 and t.shape[0] >= n2 + 1 and t.shape[1] >= n1 + 1
+    lib().orc_sat_mt(_p32(t), n1, n2, t.shape[1], threads or os.cpu_count() or 1)
     return t
 
 

@@ -50,3 +50,11 @@ def test_sat_oracle_empty_is_identity():
     t = np.arange(20, dtype=np.int32).reshape(4, 5)
     np.testing.assert_array_equal(O.sat(t, 0, 3), t)
     np.testing.assert_array_equal(O.sat(t, 4, 0), t)
+
+
+@pytest.mark.parametrize("threads", [1, 3, 8])
+def test_sat_oracle_threaded_equals_sequential(threads):
+    rng = np.random.default_rng(77 + threads)
+    for n1, n2, pad in [(1, 1, 0), (5, 9, 3), (1024, 40, 3), (2500, 33, 7), (3, 2000, 0)]:
+        t = rng.integers(-2 ** 31, 2 ** 31, (n2 + 2, n1 + 1 + pad), dtype=np.int64).astype(np.int32)
+        np.testing.assert_array_equal(O.sat_mt(t, n1, n2, threads), O.sat(t, n1, n2))
