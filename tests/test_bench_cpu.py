@@ -29,3 +29,15 @@ def test_reference_arm_line(workload):
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["config"]["workload"]
+
+
+def test_sat_cpu_baseline_helper():
+    """The SAT workload's cpu_baseline leg (host only): repeated samples, all threads."""
+    import importlib.util
+    import numpy as np
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(REPO, "bench.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    h = np.random.default_rng(2).integers(0, 10000, (300, 1027), dtype=np.int32)
+    c = b.sat_cpu_baseline(h, 1024, 298, 1027, target_s=0.2)
+    assert c["value"] > 0 and c["kind"] == "port" and c["cores"] >= 1 and " x " in c["sample"]
