@@ -343,6 +343,8 @@ def run_gme(args):
     cfg = dict(cfg)
     cfg.update({"l2": "flushed between timed steps (256 MiB write)", "plain_config": ctx.plain_config(n1, n2),
                 "parity_vs_oracle": "ok" if parity else "MISMATCH", "score": int(res.score)})
+    if kind == 2:
+        cfg["sw_max"] = {"value": int(res.sw_max), "y": int(res.sw_max_y), "x": int(res.sw_max_x)}
     line = {"metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * mean_s,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
@@ -907,6 +909,21 @@ def also_batched_served(args):
     summed-area table (the reference's SAT case)."""
     import copy
     out = {}
+    # the other single-pair workloads on the plain path: LCS 8192^2 and SW 32768^2
+    for name in ("lcs8192", "sw32768"):
+        a = copy.copy(args)
+        a.workload, a.steps, a.warmup, a.no_cpu = name, 20, 3, True
+        try:
+            p = run_gme(a)
+            c = p["config"]
+            out[name] = {"workload": c["workload"], "value": p["value"], "unit": "GCUPS",
+                         "ms_per_step": p["ms_per_step"], "e2e": p["e2e"]["value"],
+                         "roofline": {k: p["roofline"][k] for k in
+                                      ("bound", "achieved", "peak", "unit", "frac", "ops_per_cell")},
+                         "plain_config": c["plain_config"], "parity_vs_oracle": c["parity_vs_oracle"],
+                         "score": c["score"], "gpu_launches": p["gpu_launches"], "clocks": p["clocks"]}
+        except Exception as e:  # the headline line stands on its own
+            out[name] = {"error": repr(e)[:300]}
     a = copy.copy(args)
     a.steps, a.warmup, a.no_cpu, a.pairs, a.batch_warps, a.int32 = 10, 3, True, 16384, 0, False
     b = run_gme_batch(a)

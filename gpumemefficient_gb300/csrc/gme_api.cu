@@ -435,7 +435,12 @@ gme_status gme_sat_device(gme_context *ctx, int32_t *d_table, int64_t n1, int64_
   if (!ctx || (n1 > 0 && n2 > 0 && !d_table)) return GME_ERR_INVALID;
   cudaSetDevice(ctx->device);
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
-  return to_status(gme::sat_run(ctx->ws, d_table, n1, n2, ld, d_status, st, ctx->timeout_ns));
+  // a regrow of the tagged scratch must drain the stream this call runs on
+  cudaStream_t prev = ctx->ws.sync_stream;
+  ctx->ws.sync_stream = st;
+  const int rc = gme::sat_run(ctx->ws, d_table, n1, n2, ld, d_status, st, ctx->timeout_ns);
+  ctx->ws.sync_stream = prev;
+  return to_status(rc);
 }
 
 gme_status gme_sat(gme_context *ctx, int32_t *table, int64_t n1, int64_t n2, int64_t ld) {

@@ -27,9 +27,13 @@
 //      D_y(x) back in place;
 //   3. one lane per column walks the block's rows: t += D, stored to the table.
 // A pad word per 32 columns keeps both shared-memory patterns free of bank
-// conflicts.  Words are 64 bits: {tag (31 bits) | inclusive (1 bit), value}, one
-// per strip and row, tagged per call so that nothing needs clearing.  The table is
-// read and written once: 8 bytes per cell of HBM traffic.
+// conflicts.  Words are 64 bits: {tag, value}, one per strip and row.  Each call
+// takes two fresh tags from the context's counter, T for aggregates and T + 1 for
+// inclusive carries, stored as the word's whole high half: the same format and the
+// same counter as the plain kernel's band words, which share this scratch, so no
+// word left by one call can pass for a word of a later call of either kind and
+// nothing needs clearing.  The table is read and written once: 8 bytes per cell of
+// HBM traffic.
 #include <algorithm>
 
 #include "gme_common.cuh"
@@ -69,8 +73,8 @@ struct SatParams {
   int strips;
   unsigned long long *carry;  // carry[s * cstride + y]: strip s's word for row y
   long long cstride;
-  unsigned tag;
-  int *ctrl;  // [0] strip ticket, [1] status
+  unsigned tag;  // aggregates carry tag, inclusive carries tag + 1
+  int *ctrl;     // [0] strip ticket, [1] status
   unsigned long long timeout_ns;
 };
 
@@ -111,7 +115,7 @@ __global__ void __launch_bounds__(SAT_THREADS) sat_kernel(SatParams P) {
     unsigned col = xok ? (unsigned)P.table[x] : 0u;  // row 0
     unsigned long long *own = P.carry + (long long)s * P.cstride;
     const bool publish = s + 1 < P.strips;
-    const unsigned tagw = (P.tag & 0x7fffffffu) << 1;  // the word's high half; bit 0: inclusive
+    const unsigned tag_agg = P.tag, tag_inc = P.tag + 1u;  // the words' high halves
     auto issue = [&](long long b) {
       if (b < nblk) {
         int *t = sat_smem + (int)(b % SAT_STAGES) * (SAT_RB * SAT_PITCH) + sat_col(tid);
@@ -131,7 +135,8 @@ __global__ void __launch_bounds__(SAT_THREADS) sat_kernel(SatParams P) {
     for (long long b = 0; b < nblk; ++b) {
       cp_async_wait<SAT_STAGES - 2>();  // this thread's copies of block b have landed
       __syncthreads();                  // (1) everyone's have; the stage of block b-1 is free
-      if (s_abort) break;
+      // (no abort test here: the abort word is only set inside the look-back wait,
+      // between barriers (1) and (2), and barrier (2) decides for the whole CTA)
       issue(b + SAT_STAGES - 1);
       int *tile = sat_smem + (int)(b % SAT_STAGES) * (SAT_RB * SAT_PITCH);
       const long long y0 = 1 + b * SAT_RB;
@@ -163,7 +168,7 @@ __global__ void __launch_bounds__(SAT_THREADS) sat_kernel(SatParams P) {
         if (s == 0) {
           if (live[q]) c[q] = (unsigned)P.table[yq[q] * ld] - (unsigned)P.table[(yq[q] - 1) * ld];
         } else if (live[q] && publish) {
-          st_relaxed_gpu_u64(own + yq[q], ((unsigned long long)tagw << 32) | inc[q]);
+          st_relaxed_gpu_u64(own + yq[q], ((unsigned long long)tag_agg << 32) | inc[q]);
         }
       }
       // look back for every row of this lane at once
@@ -174,10 +179,12 @@ __global__ void __launch_bounds__(SAT_THREADS) sat_kernel(SatParams P) {
             if (!done[q]) {
               const unsigned long long wv = ld_relaxed_gpu_u64(P.carry + jq[q] * P.cstride + yq[q]);
               const unsigned hi = (unsigned)(wv >> 32);
-              if ((hi & ~1u) == tagw) {
+              if (hi == tag_inc) {
                 c[q] += (unsigned)wv;
-                if (hi & 1u) done[q] = true;
-                else --jq[q];  // an aggregate: strip j's own total; keep looking left
+                done[q] = true;
+              } else if (hi == tag_agg) {
+                c[q] += (unsigned)wv;
+                --jq[q];  // an aggregate: strip j's own total; keep looking left
               }
             }
           }
@@ -191,14 +198,16 @@ __global__ void __launch_bounds__(SAT_THREADS) sat_kernel(SatParams P) {
 #pragma unroll
       for (int q = 0; q < SAT_RPT; ++q) {
         if (live[q] && publish && !failed)
-          st_relaxed_gpu_u64(own + yq[q], ((unsigned long long)(tagw | 1u) << 32) | (c[q] + inc[q]));
+          st_relaxed_gpu_u64(own + yq[q], ((unsigned long long)tag_inc << 32) | (c[q] + inc[q]));
         const unsigned off = __shfl_sync(FULL, c[q], (lane & ~(SAT_SEG - 1)) | (SAT_SEG - 1)) + seg_excl[q];
         int *rowp = tile + (rr + 32 * q) * SAT_PITCH + 33 * g;
 #pragma unroll
         for (int i = 0; i < 32; ++i) rowp[i] = (int)(pv[q][i] + off);
       }
-      __syncthreads();  // (2) D_y(x) in place
-      if (s_abort) break;
+      // (2) D_y(x) in place.  The barrier also ORs every thread's own failure, so all
+      // warps take the same branch even when one gives up while another is between
+      // the barriers
+      if (__syncthreads_or(failed)) break;
       // 3. column pass: t[y][x] = t[y-1][x] + D_y(x)
       const int *cp = tile + sat_col(tid);
       int *dst = P.table + y0 * ld + x;
@@ -250,8 +259,9 @@ int sat_run(Workspace &ws, int *d_table, long long n1, long long n2, long long l
   const long long cstride = (n2 + 1 + 3) / 4 * 4;
   int rc = ws.reserve(0, 0, strips * cstride, 0);
   if (rc != ST_OK) return rc;
-  // the words carry 31 bits of tag: clear them before the counter gets there
-  if ((unsigned long long)ws.tag_next + 2ull >= 0x7fffffffull) {
+  // two tags per call from the counter the plain kernel's band words use: clear the
+  // words before the 32-bit counter wraps
+  if ((unsigned long long)ws.tag_next + 3ull >= 0xffffffffull) {
     if ((e = cudaMemsetAsync(ws.slots, 0, ws.slots_bytes, st)) != cudaSuccess)
       return ws.fail(e, "cudaMemsetAsync(slots)");
     ws.tag_next = 1;
@@ -264,7 +274,8 @@ int sat_run(Workspace &ws, int *d_table, long long n1, long long n2, long long l
   P.strips = (int)strips;
   P.carry = ws.slots;
   P.cstride = cstride;
-  P.tag = ws.tag_next++;
+  P.tag = ws.tag_next;
+  ws.tag_next += 2;
   P.ctrl = ws.ctrl;
   P.timeout_ns = timeout_ns;
   if ((e = cudaMemsetAsync(ws.ctrl, 0, 2 * sizeof(int), st)) != cudaSuccess)

@@ -290,7 +290,10 @@ gme_status gme_align_path(gme_context *ctx, gme_kind kind, const int32_t *a, int
  * receives 0 or GME_ERR_TIMEOUT when the kernel has run.  gme_sat: host table (rows
  * 0..n2 copied in and rows 1..n2 back), blocking.  Replaces the reference's
  * SOR(n1, n2, table, tX, tY) (SAT/GPU_Hyperlane_Share.h:5), which computes the same
- * table on the device but never copies it back. */
+ * table on the device but never copies it back.
+ * A context's SAT and plain-path calls share one tagged scratch buffer and one
+ * control block: calls of one context queued on different streams must be
+ * serialised by the caller (an event, or one stream for all of them). */
 gme_status gme_sat_device(gme_context *ctx, int32_t *d_table, int64_t n1, int64_t n2, int64_t ld,
                           int32_t *d_status, void *stream);
 gme_status gme_sat(gme_context *ctx, int32_t *table, int64_t n1, int64_t n2, int64_t ld);

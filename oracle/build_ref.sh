@@ -4,11 +4,14 @@
 # oracle/_ref/.  Test infrastructure only: the binaries are the checker that pins
 # the C restatement in oracle/oracle.c, never part of the product path.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
-# Exits 0 without building when the reference checkout is absent (the GPU host).
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+# The checkout is REFERENCE_ROOT, else $GME_REFERENCE_ROOT, else a directory named
+# `reference` beside this repository's own directory.  Exits 0 without building
+# when none of them holds the sources (the GPU host has no checkout).
 set -euo pipefail
-REF="${1:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
+REPO="$(dirname "$HERE")"
+REF="${1:-${GME_REFERENCE_ROOT:-$(dirname "$REPO")/reference}}"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/LCS/LCS.cpp" ]; then
   echo "build_ref: reference sources not present at $REF; skipping" >&2

@@ -1,7 +1,9 @@
 """Regenerates the golden fixtures in this directory from the reference checkout.
 
-Run here (where the read-only reference checkout exists), never on the GPU host:
-    oracle/build_ref.sh && python tests/golden/make_golden.py [REFERENCE_ROOT]
+Run where the read-only reference checkout exists, never on the GPU host:
+    oracle/build_ref.sh [REFERENCE_ROOT] && python tests/golden/make_golden.py [REFERENCE_ROOT]
+The checkout is REFERENCE_ROOT, else $GME_REFERENCE_ROOT, else a directory named
+`reference` beside this repository's own directory.
 
 Outputs
   fixture_2_15.bin  the reference's square fixture LCS/Data/str1_2_15_str2_2_15.txt
@@ -29,7 +31,19 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+
+
+def reference_root():
+    """The reference checkout: the first argument, $GME_REFERENCE_ROOT, or the
+    directory `reference` beside this repository."""
+    for cand in (sys.argv[1] if len(sys.argv) > 1 else None, os.environ.get("GME_REFERENCE_ROOT"),
+                 os.path.join(os.path.dirname(REPO), "reference")):
+        if cand and os.path.isfile(os.path.join(cand, "LCS", "LCS.cpp")):
+            return cand
+    sys.exit("make_golden: no reference checkout (pass its root or set GME_REFERENCE_ROOT)")
+
+
+REF = reference_root()
 DATA = os.path.join(REF, "LCS", "Data")
 REFBIN = os.path.join(REPO, "oracle", "_ref")
 

@@ -96,3 +96,29 @@ def test_sat_8192_closed_form(gme_ctx):
         got = d.cpu().numpy()
     want = O.sat_py(t, n1, n2)
     np.testing.assert_array_equal(got, want)
+
+
+def test_sat_tags_never_pass_for_band_rows():
+    """SAT carries and the plain kernel's band rows share one tagged scratch buffer
+    and one tag counter.  On one context whose scratch is already large (so nothing
+    is regrown and no tag is reset): a big alignment, then SAT calls, each followed
+    by an alignment with more bands than the tags the SAT calls took.  No SAT word
+    may be read as a band row, so every score and last row equals the oracle's."""
+    import os
+    import gpumemefficient_gb300 as g
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(4242)
+    with g.Context(0) as ctx:
+        a = rng.integers(0, 4, 40000).astype(np.int32)
+        b = rng.integers(0, 4, 40000).astype(np.int32)
+        assert ctx.align("ed", a, b).score == O.align(O.ED, a, b, threads=threads)["score"]
+        for i in range(3):
+            n1, n2 = 2000 + 129 * i, 30000
+            t = _table(rng, n1, n2, n1 + 3)
+            np.testing.assert_array_equal(ctx.sat(t.copy(), n1, n2), O.sat(t, n1, n2))
+            a = rng.integers(0, 4, 30000).astype(np.int32)
+            b = rng.integers(0, 4, 60000).astype(np.int32)
+            r = ctx.align("ed", a, b, last_row=True)
+            o = O.align(O.ED, a, b, threads=threads)
+            assert r.score == o["score"], i
+            np.testing.assert_array_equal(r.last_row, o["last_row"])
