@@ -337,7 +337,7 @@ gme_status gme_set_plain_config(gme_context *ctx, const gme_plain_config *cfg) {
   if (!cfg) { ctx->cfg = gme_plain_config{}; return GME_OK; }
   if ((cfg->rows_per_lane || cfg->warps_per_band) &&
       !gme::plain_config_valid(cfg->rows_per_lane, cfg->warps_per_band)) {
-    ctx->ws.last_error = "plain config: rows_per_lane must be 4, warps_per_band 1, 2, 3, 4, 6 or 8";
+    ctx->ws.last_error = "plain config: rows_per_lane must be 2 or 4, warps_per_band 4 or 8";
     return GME_ERR_INVALID;
   }
   if (cfg->grid < 0) return GME_ERR_INVALID;

@@ -40,7 +40,8 @@ constexpr long long kChunk = 16;               // columns per ring transaction
 constexpr long long words(long long bytes) { return (bytes + 255) / 256 * 32; }  // 256-byte granules
 constexpr long long kCtrlWords = words(16 * sizeof(int));
 constexpr long long kBestWords = words(kMaxGrid * 32);
-constexpr long long kAWords = words((kPadL + kMaxLen + kPadR) * sizeof(int));
+// the staged a[] and its copy shifted by two, each rounded to whole 16-byte groups
+constexpr long long kAWords = words(2 * ((kPadL + kMaxLen + kPadR + 3) / 4 * 4) * sizeof(int));
 constexpr long long kBWords = words((kMaxLen + kMaxBandRows) * sizeof(int));
 constexpr long long kStride = ((kMaxLen + 1 + kChunk - 1) / kChunk) * kChunk + kChunk;
 constexpr long long kSlotWords = (kMaxGrid + 2) * kStride;

@@ -237,7 +237,7 @@ def header_from_json(path=TUNED_JSON):
 
 # ---- the plain path: one pair per call --------------------------------------------
 PLAIN_SIZES = [2048, 4096, 8192, 16384, 32768, 65536]
-PLAIN_SHAPES = [(4, 1), (4, 2), (4, 4), (4, 8), (2, 4), (2, 8)]
+PLAIN_SHAPES = [(4, 4), (4, 8), (2, 4), (2, 8)]
 TUNED_PLAIN_H = os.path.join(HERE, "csrc", "gme_tuned_plain.h")
 
 

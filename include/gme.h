@@ -74,8 +74,8 @@ typedef struct gme_result {
 
 /* Tuning of the plain (one pair per call) wavefront kernel. Zero fields = automatic. */
 typedef struct gme_plain_config {
-  int32_t rows_per_lane;   /* cells of one anti-diagonal held per thread: 4 */
-  int32_t warps_per_band;  /* compute warps per CTA; band height = warps*32*rows_per_lane */
+  int32_t rows_per_lane;   /* cells of one anti-diagonal held per thread: 2 or 4 */
+  int32_t warps_per_band;  /* compute warps per CTA, 4 or 8; band height = warps*32*rows_per_lane */
   int32_t grid;            /* persistent CTAs (0 = one per band, capped by residency) */
   int32_t reserved;
 } gme_plain_config;
