@@ -78,18 +78,21 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
 
 
 TOOLS = os.path.join(HERE, "tools")
-TOOL_BINS = {"gme-align": ("gme_align.cpp", True), "gme-generate": ("gme_generate.cpp", False)}
+TOOL_BINS = {"gme-align": ("gme_align.cpp", True), "gme-generate": ("gme_generate.cpp", False),
+             "gme-refcheck": ("gme_refcheck.cpp", True)}
 
 
 def build_tools() -> dict:
     """The command-line tools (host C++): gme-align (the reference's drivers on the
-    library) and gme-generate (the reference's data files from a seeded PRNG)."""
+    library), gme-generate (the reference's data files from a seeded PRNG) and
+    gme-refcheck (every reference host-function signature called once)."""
     cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
     out = {}
     for name, (src, uses_lib) in TOOL_BINS.items():
         exe = os.path.join(OUTDIR, name)
         deps = [os.path.join(TOOLS, src), os.path.join(TOOLS, "gme_datafile.h"),
-                os.path.join(REPO, "include", "gme.h")] + ([LIB] if uses_lib else [])
+                os.path.join(REPO, "include", "gme.h"),
+                os.path.join(REPO, "include", "gme_reference.h")] + ([LIB] if uses_lib else [])
         if not (os.path.exists(exe) and all(os.path.getmtime(d) <= os.path.getmtime(exe) for d in deps)):
             cmd = [shutil.which("g++") or "g++", "-O2", "-std=c++17", "-I" + os.path.join(REPO, "include"),
                    "-I" + TOOLS, os.path.join(TOOLS, src), "-o", exe + f".tmp{os.getpid()}"]

@@ -51,6 +51,7 @@ int SW(int n1, int n2, int *arr1, int *arr2, int, int, int *, int, int) { return
 int SW(int n1, int n2, int *arr1, int *arr2, int, int, int *) { return run(GME_SW, n1, n2, arr1, arr2); }
 int SW(int n1, int n2, int *arr1, int *arr2) { return run(GME_SW, n1, n2, arr1, arr2); }
 void SOR(int n1, int n2, int *table, int, int) { run_sat(n1, n2, table); }
+void SOR(int n1, int n2, int *table) { run_sat(n1, n2, table); }
 
 extern "C" {
 gme_status gme_reference_last_status(void) { return g_last; }

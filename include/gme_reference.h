@@ -47,12 +47,14 @@ int SW(int n1, int n2, int *arr1, int *arr2, int paddX, int paddY, int *table, i
 int SW(int n1, int n2, int *arr1, int *arr2, int paddX, int paddY, int *table);
 /* SmithWaterman/GPU.h:5 */
 int SW(int n1, int n2, int *arr1, int *arr2);
-/* SAT/GPU_Hyperlane_Share.h:5, SAT/GPU_Hyperlane_Cache.h:5: the summed-area table of
- * the reference's layout (rows 0..n2, row length n1 + 3; gme_sat).  Unlike the
- * reference, which leaves `table` untouched (its copy back is commented out,
- * SAT/GPU_Hyperlane_Share.cu:321), rows 1..n2 x columns 1..n1 of `table` receive
- * the result.  tX, tY are accepted and ignored. */
+/* SAT/GPU_Hyperlane_Share.h:5: the summed-area table of the reference's layout (rows
+ * 0..n2, row length n1 + 3; gme_sat).  Unlike the reference, which leaves `table`
+ * untouched (its copy back is commented out, SAT/GPU_Hyperlane_Share.cu:321), rows
+ * 1..n2 x columns 1..n1 of `table` receive the result.  tX, tY are accepted and
+ * ignored. */
 void SOR(int n1, int n2, int *table, int tX, int tY);
+/* SAT/GPU_Hyperlane_Cache.h:5: the same, in the Cache driver's three-argument form. */
+void SOR(int n1, int n2, int *table);
 #endif
 
 #ifdef __cplusplus
