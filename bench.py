@@ -548,7 +548,8 @@ def run_gme_served(args):
     cells = float(cells_k.sum())
     ops = float(sum(cells_k[kinds == k].sum() * OPS_PER_CELL[k] for k in range(3)))
     sc = g.scoring()
-    srv = g.Server(local, sc=sc, waves=args.waves, wave_max_cells=args.wave_cells)
+    mode = g.SERVE_WAVES if args.serve_mode == "waves" else g.SERVE_RING
+    srv = g.Server(local, sc=sc, waves=args.waves, wave_max_cells=args.wave_cells, mode=mode)
 
     # parity of every request with the oracle (outside the timed region)
     tick = srv.submit_many(symbols, pairs)
@@ -656,7 +657,8 @@ def run_gme_served(args):
     roof = {"bound": "int_alu", "achieved": achieved, "peak": peak_tops, "unit": "Tops/s",
             "frac": achieved / peak_tops, "traffic": None,
             "peak_basis": f"{sms} SMs x {INT_LANES_PER_SM} INT32 lanes x median SM clock {mhz:.0f} MHz under load",
-            "ops_per_cell": "ED 7, SW 8 weighted by cells", "kernel": "batch_kernel (served, host clock)"}
+            "ops_per_cell": "ED 7, SW 8 weighted by cells",
+            "kernel": ("serve_kernel" if mode == g.SERVE_RING else "batch_kernel") + " (served, host clock)"}
     cpu = None
     if rank == 0 and not args.no_cpu:
         k = min(n, 400)
@@ -668,10 +670,13 @@ def run_gme_served(args):
                                          f"oracle/oracle.c pairs across {os.cpu_count()} threads, {dt:.2f} s"}
     h2d = int(symbols.nbytes + n * (pairs.itemsize + 64))
     d2h = int(n * (g.RESULT_DTYPE.itemsize + 4))
+    how = ("one persistent kernel taking jobs from device-resident rings" if mode == g.SERVE_RING else
+           "waves of the batched kernel on launch slots on separate streams")
     cfg = {"workload": f"served: {n} requests per step, half ED half SW, lengths log-uniform [32, 16384], "
-                       "alphabet 4, submitted open loop to the server (host queue, HBM-budget admission, "
-                       "launch slots on separate streams, completion flags in pinned memory); value = "
-                       "sustained throughput with `steps` passes of the stream submitted back to back",
+                       f"alphabet 4, submitted open loop to the server (host queue, HBM-budget admission, {how}, "
+                       "completion flags in pinned memory); value = sustained throughput with `steps` passes "
+                       "of the stream submitted back to back",
+           "serve_mode": args.serve_mode,
            "requests": n, "cells": cells, "seed": synth.SEED_SERVE, "hbm_budget_bytes": st1["hbm_budget_bytes"],
            "hbm_bytes_peak": st1["hbm_bytes_peak"], "waves_per_step": (st1["waves_launched"] - st0["waves_launched"]) / len(times),
            "l2": "inputs (172 MB of symbols per step) larger than L2", "parity_vs_oracle": {True: "ok", False: "MISMATCH", None: "skipped"}[parity],
@@ -871,8 +876,10 @@ def main():
                         "16 bits on the packed s16x2 engine)")
     p.add_argument("--requests", type=int, default=8192, help="served workload: requests per step")
     p.add_argument("--waves", type=int, default=0, help="served workload: launch slots (0 = default)")
-    p.add_argument("--rates", type=float, nargs="*", default=[0.1, 0.5, 0.8],
+    p.add_argument("--rates", type=float, nargs="*", default=[0.1, 0.3, 0.5, 0.7, 0.9, 1.0, 1.2],
                    help="served workload: offered load as fractions of the saturation throughput")
+    p.add_argument("--serve-mode", default="ring", choices=["ring", "waves"],
+                   help="served workload: persistent kernel on device job rings, or waves of launches")
     p.add_argument("--rate-seconds", type=float, default=2.0, help="served workload: seconds per rate point")
     p.add_argument("--wave-cells", type=int, default=0, help="served workload: cells per launch at most (0 = default)")
     p.add_argument("--no-parity", action="store_true", help="skip the oracle parity check (tuning runs)")
@@ -936,7 +943,7 @@ def also_batched_served(args):
                       "gpu_launches": b["gpu_launches"], "clocks": b["clocks"]}
     a = copy.copy(args)
     a.steps, a.warmup, a.no_cpu, a.requests, a.waves, a.wave_cells = 5, 3, True, 8192, 0, 0
-    a.rates, a.rate_seconds, a.no_parity = [0.1, 0.5, 0.8], 1.5, False
+    a.rates, a.rate_seconds, a.no_parity, a.serve_mode = [0.1, 0.5, 0.8, 1.0], 1.5, False, "ring"
     s = run_gme_served(a)
     c = s["config"]
     out["served"] = {"workload": c["workload"], "value": s["value"], "unit": "GCUPS",

@@ -70,7 +70,10 @@ RESULT_DTYPE = np.dtype([("score", "<i4"), ("sw_max", "<i4"), ("sw_max_y", "<i8"
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("wave_max_cells", ctypes.c_int64),
                 ("waves", ctypes.c_int32), ("queue_max", ctypes.c_int32),
-                ("warps_per_block", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("warps_per_block", ctypes.c_int32), ("mode", ctypes.c_int32)]
+
+
+SERVE_RING, SERVE_WAVES = 0, 1
 
 
 class ServerStats(ctypes.Structure):
@@ -360,17 +363,19 @@ class BatchPlan:
 class Server:
     """The served path: submit alignments one at a time, collect each as it finishes.
 
-    A native dispatcher thread admits queued requests against the HBM budget and
-    launches them in waves on several streams; results and completion flags come
-    back through pinned host memory (``include/gme.h``, served path).
+    A native dispatcher thread admits queued requests against the HBM budget.  In ring
+    mode (the default) a persistent kernel takes them from device-resident job rings as
+    they are published; in waves mode they run as launches of the batched kernel on
+    several streams.  Results and completion flags come back through pinned host memory
+    (``include/gme.h``, served path).
     """
 
     NOT_READY = 7
 
     def __init__(self, device: int = 0, sc: Optional[Scoring] = None, hbm_budget_bytes: int = 0,
                  wave_max_cells: int = 0, waves: int = 0, queue_max: int = 0,
-                 warps_per_block: int = 0):
-        cfg = ServerConfig(hbm_budget_bytes, wave_max_cells, waves, queue_max, warps_per_block, 0)
+                 warps_per_block: int = 0, mode: int = SERVE_RING):
+        cfg = ServerConfig(hbm_budget_bytes, wave_max_cells, waves, queue_max, warps_per_block, mode)
         self.sc = sc or scoring()
         h = ctypes.c_void_p()
         _check(lib().gme_server_create(device, ctypes.byref(cfg), ctypes.byref(self.sc),

@@ -58,6 +58,18 @@ struct __align__(16) TeamSlot {
   int done;                 // members finished
 };
 
+// A large pair of the served kernel, shared by the CTAs that take its entries in the
+// CTA ring: each claims the pair's next band group (next) and sweeps it with its warps,
+// group g taking its incoming row from group g-1's CTA through two tagged rows.  A CTA
+// waits only on groups claimed before its own, each on a running CTA, so a team never
+// waits on an entry no CTA has taken.  The CTA that finishes the last group (gdone)
+// writes the result; the last of the team's entries to leave (left) raises the team's
+// release flag in mapped host memory, after which the host may reuse the team.
+struct __align__(16) ServeTeam {
+  unsigned long long best;  // SW: as TeamSlot::best
+  int next, gdone, left, corner;
+};
+
 struct BatchParams {
   const int *sym;          // staged, padded symbols
   const BatchJob *jobs_b;  // block jobs, by kind, longest first
@@ -81,6 +93,18 @@ struct BatchParams {
   int *ctrl;               // [2k] block ticket of kind k, [2k+1] warp ticket, [8] status, [10+k] team ticket
   Scoring sc;
   unsigned long long timeout_ns;
+  // the served kernel's job rings (serve_kernel): the ring words (RW_*), the
+  // rings' slots (jobs_b and jobs_w hold each kind's ring after the last's); per
+  // CTA-ring slot, units[] holds {team, tag0, entries of the pair, 0} (entries 1: the
+  // pair runs on the CTA alone); teams, their wrap rows and release flags
+  ServeTeam *steam;
+  int *tfree;
+  int *cq;                 // optional: each job's result slot + 1, appended once it is done
+  unsigned *cq_n;          //   (mapped host memory) at cq[(*cq_n)++ & cq_mask]
+  int cq_mask;
+  int *ring_ctl;
+  int qb, qw;
+  unsigned long long idle_ns;
 };
 
 template <int NW> struct __align__(16) BatchSmem {
@@ -509,9 +533,11 @@ __device__ __forceinline__ int job_status(const BatchParams &P, const int &abort
 // scope so that a host thread polling the flag in mapped memory sees the result.
 __device__ __forceinline__ void put_result(const BatchParams &P, int index, const gme_result &r) {
   P.results[index] = r;
-  if (P.done) {
-    __threadfence_system();
-    *(volatile int *)&P.done[index] = 1;
+  if (P.done || P.cq) __threadfence_system();
+  if (P.done) *(volatile int *)&P.done[index] = 1;
+  if (P.cq) {
+    const unsigned pos = atomicAdd(P.cq_n, 1u);
+    *(volatile int *)&P.cq[pos & (unsigned)P.cq_mask] = index + 1;
   }
 }
 
@@ -622,6 +648,19 @@ __device__ void warp_job(const BatchParams &P, BatchSmem<NW> &S, const BatchJob 
   const int *a_sym = P.sym + jb.a_off;
   const int *b_sym = P.sym + jb.b_off;
   const int nb = (M + 32 * R - 1) / (32 * R);
+  if (N == 0 || M == 0) {
+    // an empty sequence: the table is its borders (the served kernel takes such pairs)
+    if (lane == 31) {
+      gme_result r;
+      r.score = (M == 0) ? Rec<KIND>::to_v(Rec<KIND>::top(N, P.sc.ed_rule), N, 0)
+                         : Rec<KIND>::to_v(Rec<KIND>::left(M), 0, M);
+      r.sw_max = 0; r.sw_max_y = 0; r.sw_max_x = 0;
+      r.status = job_status(P, S.abort);
+      r.kind = KIND;
+      put_result(P, jb.index, r);
+    }
+    return;
+  }
   int *row = P.rows + ((long long)blockIdx.x * NW + warp) * P.stride;
   const bool p16 = R == 4 && job_p16(P, jb);
   SwBest tb = {0, 0, 0, 0};
@@ -748,6 +787,263 @@ __global__ void __launch_bounds__(NW * 32, NW == 4 ? GME_BATCH_MIN_BLOCKS : 1) b
     }
     __syncthreads();
   }
+}
+
+// Claims the next job of a ring, if the host has published one: its ticket, or -1.
+// The tail is read with acquire semantics, so the job's descriptor and symbols
+// (copied in before the tail was published) are seen by the loads that follow.
+__device__ __forceinline__ int ring_claim(int *ctl, int k, int c) {
+  int *head = &ctl[2 * k + c];
+  int h = ld_relaxed_gpu_s32(head);
+  const int t = ld_acquire_gpu_s32(&ctl[RW_TAIL + 2 * k + c]);
+  while (h < t) {
+    const int got = atomicCAS(head, h, h + 1);
+    if (got == h) return h;
+    h = got;
+  }
+  return -1;
+}
+
+// Jobs waiting in kind k's CTA ring (c = 0) or warp ring (c = 1), as last seen.
+__device__ __forceinline__ int ring_backlog(const int *ctl, int k, int c) {
+  return ld_relaxed_gpu_s32(&ctl[RW_TAIL + 2 * k + c]) - ld_relaxed_gpu_s32(&ctl[2 * k + c]);
+}
+
+// The kind a pair of SMs runs (its word *pk): the current one while any job of it is
+// waiting, else the kind with the most work waiting (a CTA job counted as 64 warp
+// jobs), written back for the pair's other CTAs; -1 when every ring is empty.  One
+// kind per pair of SMs at a time because the three kinds' loops do not fit the
+// instruction cache the two SMs share (the batch kernel's measurement).
+__device__ int pick_kind(const int *ctl, int *pk) {
+  const int k0 = ld_relaxed_gpu_s32(pk);
+  if (ring_backlog(ctl, k0, 0) > 0 || ring_backlog(ctl, k0, 1) > 0) return k0;
+  int best = -1;
+  long long bw = 0;
+  for (int k = 0; k < 3; ++k) {
+    const long long w = 64ll * ring_backlog(ctl, k, 0) + ring_backlog(ctl, k, 1);
+    if (w > bw) { bw = w; best = k; }
+  }
+  if (best >= 0 && best != k0) atomicCAS(pk, k0, best);
+  return best;
+}
+
+// One entry of a served team (ServeTeam): band groups of the pair, claimed one at a
+// time, each swept by the CTA's warps as a block job's group is.  Group g's wrap row
+// carries tag tag0 + g + 1; the host hands each use of a team a tag0 above every tag
+// its rows hold, so they need no clearing between uses.
+template <int KIND, int R, int NW>
+__device__ void team_work(const BatchParams &P, BatchSmem<NW> &S, const BatchJob &jb, int warp, int lane,
+                          Waiter &W, ServeTeam *tm, unsigned long long *wrap, unsigned tag0, int *freed,
+                          int entries) {
+  const int N = jb.n1, M = jb.n2;
+  const int *a_sym = P.sym + jb.a_off;
+  const int *b_sym = P.sym + jb.b_off;
+  const int nb = (M + 32 * R - 1) / (32 * R);
+  const int G = (nb + NW - 1) / NW;
+  const bool p16 = R == 4 && job_p16(P, jb);
+  for (;;) {
+    if (threadIdx.x == 0) S.phase = *(volatile int *)&S.abort ? G : atomicAdd(&tm->next, 1);
+    for (int i = threadIdx.x; i < NW * (RING / CB); i += blockDim.x) (&S.tag[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < NW; i += blockDim.x) S.cons[i] = 0;
+    __syncthreads();
+    const int g = S.phase;
+    if (g >= G) break;
+    const int band = g * NW + warp;
+    SwBest tb = {0, 0, 0, 0};
+    if (band < nb) {
+      Src in;
+      in.rule = P.sc.ed_rule;
+      if (band == 0) {
+        in.mode = IN_TOP;
+      } else if (warp == 0) {
+        in.mode = IN_ROW; in.row = wrap + ((g - 1) & 1) * P.stride; in.tag = tag0 + g;
+      } else {
+        in.mode = IN_RING; in.buf = S.ring[warp]; in.tags = S.tag[warp]; in.cons = &S.cons[warp]; in.base = 0;
+      }
+      Dst out;
+      out.cons_seen = 0;
+      if (band == nb - 1) {
+        last_row_dst<KIND>(P, jb, out);
+      } else if (warp == NW - 1) {
+        out.mode = OUT_ROW; out.row = wrap + (g & 1) * P.stride; out.tag = tag0 + g + 1;
+      } else {
+        out.mode = OUT_RING; out.buf = S.ring[warp + 1]; out.tags = S.tag[warp + 1];
+        out.cons = &S.cons[warp + 1]; out.base = 0;
+      }
+      int c = 0;
+      sweep_job_band<KIND, R>(p16, P.sc, a_sym, b_sym, N, M, band * 32 * R, lane, in, out, W, c, tb,
+                              col_dst<KIND>(P, jb, band, lane));
+      if (band == nb - 1 && lane == 31) {
+        *(volatile int *)&tm->corner = c;
+        __threadfence();
+      }
+    }
+    if (KIND == K_SW) {
+      tb = warp_best(tb);
+      if (lane == 0) S.best[warp] = tb;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (KIND == K_SW) {
+        SwBest b = {0, 0, 0, 0};
+        for (int k = 0; k < NW; ++k)
+          if (better(S.best[k], b)) b = S.best[k];
+        if (b.v > 0)
+          atomicMax(&tm->best, ((unsigned long long)(unsigned)b.v << 32) |
+                                   (0xffffffffu - (unsigned)(b.y * (N + 1) + b.x)));
+      }
+      __threadfence();
+      if (atomicAdd(&tm->gdone, 1) == G - 1) {
+        __threadfence();
+        gme_result r;
+        r.score = Rec<KIND>::to_v(*(volatile int *)&tm->corner, N, M);
+        const unsigned long long k = KIND == K_SW ? atomicAdd(&tm->best, 0ull) : 0ull;
+        r.sw_max = (int)(k >> 32);
+        const long long lin = r.sw_max ? (long long)(0xffffffffu - (unsigned)k) : 0;
+        r.sw_max_y = r.sw_max ? lin / (N + 1) : 0;
+        r.sw_max_x = r.sw_max ? lin % (N + 1) : 0;
+        r.status = job_status(P, S.abort);
+        r.kind = KIND;
+        put_result(P, jb.index, r);
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&tm->left, 1) == entries - 1) {
+      __threadfence_system();
+      *(volatile int *)freed = 1;
+    }
+  }
+}
+
+// The served path's persistent kernel.  Launched once and left running while work
+// arrives.  Jobs wait in six rings, a CTA ring (large pairs, the CTA's warps pipelined
+// over the pair's bands, as block jobs of the batch kernel; the largest shared by a
+// team of CTAs, ServeTeam) and a warp ring (small pairs, one per warp) per kind.  A CTA takes the next job of its SM pair's kind's CTA
+// ring; when there is none, its warps take jobs of that kind's warp ring one after
+// another, each on its own, and regroup once a CTA job of the kind is waiting and a
+// slice of SLICE_NS has passed, or once no warp job is left.  The host appends jobs and
+// publishes each ring's tail; results and completion flags go to mapped host memory as
+// the batch kernel writes them.
+// The kernel leaves as a whole: when the host sets the stop word, when a bounded wait
+// anywhere has given up (the status word), or when no CTA has found a job for idle_ns
+// (the time of the last claim; the first CTA to see it expire raises the exit word and
+// no CTA claims a job after that).  The host launches the kernel again when it has
+// work and the last launch has ended.
+#ifndef GME_SERVE_SLICE_NS
+#define GME_SERVE_SLICE_NS 4000000ull
+#endif
+constexpr unsigned long long SLICE_NS = GME_SERVE_SLICE_NS;
+
+template <int R, int NW>
+__global__ void __launch_bounds__(NW * 32, NW == 4 ? GME_BATCH_MIN_BLOCKS : 1) serve_kernel(BatchParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  BatchSmem<NW> &S = *reinterpret_cast<BatchSmem<NW> *>(smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int *ctl = P.ring_ctl;
+  unsigned long long *last = reinterpret_cast<unsigned long long *>(ctl + RW_LAST);
+  unsigned smid;
+  asm("mov.u32 %0, %%smid;" : "=r"(smid));
+  int *pk = ctl + RW_PAIR + (int)((smid >> 1) % (unsigned)RW_PAIRS);
+  if (threadIdx.x == 0) {
+    S.abort = 0;
+    atomicMax(last, globaltimer_ns());
+  }
+  __syncthreads();
+  Waiter W(P.timeout_ns, &P.ctrl[8], &S.abort);
+  auto stopping = [&]() {
+    return *(volatile int *)&S.abort || ld_relaxed_gpu_s32(&ctl[RW_STOP]) != 0 ||
+           ld_relaxed_gpu_s32(&ctl[RW_EXIT]) != 0 || ld_relaxed_gpu_s32(&P.ctrl[8]) != 0;
+  };
+  for (;;) {
+    if (threadIdx.x == 0) {
+      int job = -2;
+      if (!stopping()) {
+        const int k = pick_kind(ctl, pk);
+        const int t = k >= 0 ? ring_claim(ctl, k, 0) : -1;
+        const unsigned long long now = globaltimer_ns();
+        if (t >= 0) {
+          atomicMax(last, now);
+          job = k * P.qb + t % P.qb;
+          // a pair on this CTA alone: tags for its wrap rows, one per band group, never
+          // used before
+          if (P.units[job].z == 1) {
+            const int n2 = P.jobs_b[job].n2;
+            S.gen = atomicAdd(P.gen, (unsigned)((n2 + 32 * R * NW - 1) / (32 * R * NW)));
+          }
+        } else if (k < 0 && now > ld_relaxed_gpu_u64(last) + P.idle_ns) {
+          atomicExch(&ctl[RW_EXIT], 1);
+        } else {
+          job = -1;
+        }
+      }
+      S.job = job;
+    }
+    for (int i = threadIdx.x; i < NW * (RING / CB); i += blockDim.x) (&S.tag[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < NW; i += blockDim.x) S.cons[i] = 0;
+    __syncthreads();
+    const int job = S.job;
+    if (job == -2) break;
+    if (job >= 0) {
+      const BatchJob jb = P.jobs_b[job];
+      const int4 u = P.units[job];
+      if (u.z > 1) {
+        ServeTeam *tm = P.steam + u.x;
+        unsigned long long *tw = P.twrap + (long long)u.x * 2 * P.stride;
+        int *fr = P.tfree + u.x;
+        switch (jb.kind) {
+          case K_LCS: team_work<K_LCS, R, NW>(P, S, jb, warp, lane, W, tm, tw, (unsigned)u.y, fr, u.z); break;
+          case K_ED: team_work<K_ED, R, NW>(P, S, jb, warp, lane, W, tm, tw, (unsigned)u.y, fr, u.z); break;
+          default: team_work<K_SW, R, NW>(P, S, jb, warp, lane, W, tm, tw, (unsigned)u.y, fr, u.z); break;
+        }
+      } else {
+        unsigned long long *wrap = P.wrap + (long long)blockIdx.x * 2 * P.stride;
+        switch (jb.kind) {
+          case K_LCS: block_job<K_LCS, R, NW>(P, S, jb, warp, lane, W, 0, 1, wrap, S.gen, nullptr); break;
+          case K_ED: block_job<K_ED, R, NW>(P, S, jb, warp, lane, W, 0, 1, wrap, S.gen, nullptr); break;
+          default: block_job<K_SW, R, NW>(P, S, jb, warp, lane, W, 0, 1, wrap, S.gen, nullptr); break;
+        }
+      }
+      __syncthreads();
+      continue;
+    }
+    // warp jobs, each warp on its own
+    const unsigned long long t0 = globaltimer_ns();
+    int ran = 0;
+    for (;;) {
+      int w = -1;
+      if (lane == 0 && !stopping()) {
+        int k = ld_relaxed_gpu_s32(pk);
+        const bool cta_waiting = ring_backlog(ctl, k, 0) > 0;
+        if (!(cta_waiting && globaltimer_ns() > t0 + SLICE_NS)) {
+          int t = ring_claim(ctl, k, 1);
+          if (t < 0 && !cta_waiting) {
+            // nothing of this kind is left: the pair moves on
+            k = pick_kind(ctl, pk);
+            if (k >= 0) t = ring_claim(ctl, k, 1);
+          }
+          if (t >= 0) {
+            atomicMax(last, globaltimer_ns());
+            w = k * P.qw + t % P.qw;
+          }
+        }
+      }
+      w = __shfl_sync(FULL, w, 0);
+      if (w < 0) break;
+      const BatchJob jb = P.jobs_w[w];
+      switch (jb.kind) {
+        case K_LCS: warp_job<K_LCS, R, NW>(P, S, jb, warp, lane, W); break;
+        case K_ED: warp_job<K_ED, R, NW>(P, S, jb, warp, lane, W); break;
+        default: warp_job<K_SW, R, NW>(P, S, jb, warp, lane, W); break;
+      }
+      ++ran;
+      if (*(volatile int *)&S.abort) break;
+    }
+    if (!__syncthreads_or(ran)) __nanosleep(2000);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) atomicAdd(&ctl[RW_EXITS], 1);
 }
 
 // Copies every pair's sequences into the padded, aligned layout the engine reads,
@@ -1018,6 +1314,7 @@ int batch_launch(Workspace &ws, BatchArena &ar, const int *d_sym, const Scoring 
                                              ar.d_total, (int)ar.nseg, ar.d_staged, ar.d_symbad);
   if ((e = cudaGetLastError()) != cudaSuccess) return ws.fail(e, "batch_stage_kernel");
   BatchParams P;
+  std::memset(&P, 0, sizeof(P));  // the served kernel's fields stay null
   P.sym = ar.d_staged;
   P.jobs_b = ar.d_jobs;
   P.jobs_w = ar.d_jobs + ar.n_b;
@@ -1077,5 +1374,70 @@ int batch_run(Workspace &ws, BatchArena &ar, const int *d_sym, long long nsym, c
   if (rc != ST_OK) return rc;
   return batch_long(ar, d_sym, d_results, d_last_rows, d_last_cols, plain, plain_ctx);
 }
+
+
+// ---------------------------------------------------------------------------
+// The served kernel (serve_kernel): its shape, grid and launch.
+// ---------------------------------------------------------------------------
+template <int NW>
+static cudaError_t serve_launch_t(const BatchParams &P, int grid, cudaStream_t st) {
+  const size_t smem = sizeof(BatchSmem<NW>);
+  cudaError_t e = cudaFuncSetAttribute(serve_kernel<4, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  serve_kernel<4, NW><<<grid, NW * 32, smem, st>>>(P);
+  return cudaGetLastError();
+}
+
+int serve_grid(int sms, int NW) {
+  int n = 0;
+  if (NW == 8) {
+    cudaFuncSetAttribute(serve_kernel<4, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BatchSmem<8>));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, serve_kernel<4, 8>, 8 * 32, sizeof(BatchSmem<8>));
+  } else {
+    cudaFuncSetAttribute(serve_kernel<4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BatchSmem<4>));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, serve_kernel<4, 4>, 4 * 32, sizeof(BatchSmem<4>));
+  }
+  return sms * std::max(n, 1);
+}
+
+cudaError_t serve_launch(const ServeArgs &a, cudaStream_t st) {
+  BatchParams P;
+  std::memset(&P, 0, sizeof(P));
+  P.sym = a.arena;
+  P.jobs_b = a.jobs_b;
+  P.jobs_w = a.jobs_w;
+  P.results = a.results;
+  P.done = a.done;
+  P.symbad = a.symbad;
+  P.packed16 = 1;
+  P.rows = a.rows;
+  P.wrap = a.wrap;
+  P.gen = a.gen;
+  P.stride = a.stride;
+  P.ctrl = a.ctrl;
+  P.sc.match = a.sc.match;
+  P.sc.mismatch = a.sc.mismatch;
+  P.sc.gap = a.sc.gap;
+  P.sc.ed_rule = a.sc.ed_boundary;
+  P.timeout_ns = a.timeout_ns;
+  P.ring_ctl = a.ring_ctl;
+  P.units = a.units;
+  P.steam = reinterpret_cast<ServeTeam *>(a.teams);
+  P.twrap = a.twrap;
+  P.tfree = a.tfree;
+  P.cq = a.cq;
+  P.cq_n = reinterpret_cast<unsigned *>(a.ring_ctl + RW_CQN);
+  P.cq_mask = a.cq_mask;
+  P.qb = a.qb;
+  P.qw = a.qw;
+  P.idle_ns = a.idle_ns;
+  return a.NW == 8 ? serve_launch_t<8>(P, a.grid, st) : serve_launch_t<4>(P, a.grid, st);
+}
+
+int serve_row_stride(int max_n1) { return row_stride(max_n1); }
+int serve_padl() { return PADL; }
+long long serve_a_len(int n1) { return (PADL + (long long)n1 + PADR + 3) / 4 * 4; }
+int serve_rows_mult(int NW, bool block) { return block ? 32 * 4 * NW : 32 * 4; }
+long long serve_team_bytes() { return sizeof(ServeTeam); }
 
 }  // namespace gme

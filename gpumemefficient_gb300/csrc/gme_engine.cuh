@@ -65,8 +65,20 @@ __device__ __forceinline__ unsigned long long entry(int pos, int v) {
   return ((unsigned long long)(unsigned)(pos + 1) << 32) | (unsigned)v;
 }
 
-__device__ __forceinline__ int4 ldg4(const int *p) { return __ldg(reinterpret_cast<const int4 *>(p)); }
-__device__ __forceinline__ int2 ldg2(const int *p) { return __ldg(reinterpret_cast<const int2 *>(p)); }
+// Symbol loads: plain (coherent) global loads, cached in L1.  Not the read-only path:
+// the served kernel runs while the host copies new pairs' symbols into its arena, and
+// the read-only path may only read data that stays constant for a kernel's lifetime.
+// Volatile, so that no load is moved ahead of the acquire that published its data.
+__device__ __forceinline__ int4 ldg4(const int *p) {
+  int4 v;
+  asm volatile("ld.global.v4.b32 {%0,%1,%2,%3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ int2 ldg2(const int *p) {
+  int2 v;
+  asm volatile("ld.global.v2.b32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+  return v;
+}
 
 // n consecutive symbols from p into d[0..n): 16-byte loads when the lane's symbol base
 // is 16-byte aligned (R a multiple of 4), else 8-byte loads (R = 2).

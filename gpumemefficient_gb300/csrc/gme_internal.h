@@ -118,6 +118,45 @@ long long batch_grid(int sms, int NW, int blocks_per_sm);
 long long batch_scratch_bytes(long long grid, int NW, int max_n1);
 // the tuned table's entry for a batch of pairs (given.user_set: `given` itself)
 BatchTuning batch_tuning_for(const gme_pair *pairs, long long npairs, const BatchTuning &given);
+// the served path's persistent kernel (gme_batch.cu, serve_kernel)
+// The served kernel's ring words (ints).  Six job rings, a CTA ring and a warp ring
+// per kind: the head of kind k's CTA ring at [2k], of its warp ring at [2k + 1], their
+// tails at [RW_TAIL + 2k] and [RW_TAIL + 2k + 1]; the stop word, CTAs that have left,
+// the exit word (raised once the kernel has been idle), the time of the last claim
+// (64 bits, nanoseconds), the completion queue's count and, per pair of SMs, the kind
+// it runs.
+constexpr int RW_TAIL = 8, RW_STOP = 16, RW_EXITS = 17, RW_EXIT = 18, RW_LAST = 20, RW_CQN = 22, RW_PAIR = 64,
+              RW_PAIRS = 128, RW_WORDS = RW_PAIR + RW_PAIRS;
+struct ServeArgs {
+  int *arena;                 // staged symbols of the jobs (offsets in BatchJob are into it)
+  BatchJob *jobs_b, *jobs_w;  // the CTA rings (kind k at k * qb) and the warp rings (k * qw)
+  int qb, qw;                 // slots of each ring
+  int *symbad;                // per job segment: 1 if a symbol lies outside [0, 32767]
+  gme_result *results;        // results and completion flags (mapped host memory)
+  int *done;
+  int *rows;                  // grid * NW rows of `stride` ints (warp jobs)
+  unsigned long long *wrap;   // grid * 2 tagged rows of `stride` words (CTA jobs)
+  unsigned *gen;              // wrap-row tags handed out (kept across launches)
+  int stride;
+  int *ctrl;                  // [8] status
+  int *ring_ctl;              // RW_WORDS ring words
+  const int4 *units;          // per CTA-ring slot: {team, tag0, the pair's entries (1: alone), 0}
+  void *teams;                // serve_team_bytes() per team, cleared before each use
+  unsigned long long *twrap;  // 2 tagged rows of `stride` words per team (tags below tag0)
+  int *tfree;                 // per team, mapped host memory: 1 once its last entry has left
+  int *cq;                    // completion queue (mapped host memory): result slot + 1 per job done
+  int cq_mask;                // its entries - 1 (a power of 2); the count is ring word RW_CQN
+  gme_scoring sc;
+  unsigned long long timeout_ns, idle_ns;
+  int NW, grid;
+};
+int serve_grid(int sms, int NW);
+int serve_row_stride(int max_n1);
+int serve_padl();                 // symbols before a's first one in its staged segment
+long long serve_a_len(int n1);    // ints of a's staged segment (pads included, 16-byte multiple)
+int serve_rows_mult(int NW, bool block);
+long long serve_team_bytes();
+cudaError_t serve_launch(const ServeArgs &a, cudaStream_t st);
 // summed-area table (gme_sat.cu)
 int sat_run(Workspace &ws, int *d_table, long long n1, long long n2, long long ld, int *d_status,
             cudaStream_t st, unsigned long long timeout_ns);

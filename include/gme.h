@@ -196,30 +196,39 @@ gme_status gme_batch_stats(const gme_context *ctx, int64_t *block_jobs, int64_t 
                            int64_t *long_jobs, int64_t *team_jobs);
 
 /* ---- served path: requests one at a time, each result as soon as it is done ----
- * A server owns a host request queue, a dispatcher thread and `waves` launch slots
- * (each a stream with its own device buffers).  gme_submit copies a request into
- * the queue and returns a ticket at once.  The dispatcher admits queued requests
- * in arrival order against the HBM budget, packs them into the next free slot
- * (symbols in one copy from pinned memory) and launches the batched work-queue
- * kernel there; the kernel writes each result and then its completion flag into
- * pinned host memory, so a request completes when its own pair is done, not when
- * its launch is.  Slots run concurrently: a new launch's CTAs take over SMs as the
- * previous launch drains.  No counterpart in the reference, whose host functions
- * align one pair per call (EditDistance/GPU_Hyperlane_Share.cu:689-789). */
+ * A server owns a host request queue and a dispatcher thread.  gme_submit copies a
+ * request into the queue and returns a ticket at once.  Two modes:
+ *   GME_SERVE_RING (the default): one persistent kernel stays resident on the GPU and
+ *     takes jobs from two device-resident rings (pairs of 2^22 cells and more, one per
+ *     CTA; the rest, one per warp).  The dispatcher admits queued requests in arrival
+ *     order while the symbol arena (the budget less the kernel's fixed rows) and the
+ *     rings have room, copies their padded symbols and descriptors in, then publishes
+ *     each ring's new tail; the kernel picks jobs up as they are published.  Each
+ *     result and then its completion flag are written into pinned host memory, so a
+ *     request completes when its own pair is done.  The kernel leaves after a short
+ *     idle time and is launched again when work arrives.  Pairs wider than 16384 (the
+ *     kernel's row width) run as launches of the batched kernel, as in the other mode.
+ *   GME_SERVE_WAVES: admitted requests form waves; each wave is one launch of the
+ *     batched work-queue kernel on one of `waves` launch slots (separate streams), up
+ *     to wave_max_cells cells and the slot's share of the budget.
+ * No counterpart in the reference, whose host functions align one pair per call
+ * (EditDistance/GPU_Hyperlane_Share.cu:689-789). */
+typedef enum gme_serve_mode { GME_SERVE_RING = 0, GME_SERVE_WAVES = 1 } gme_serve_mode;
 typedef struct gme_server gme_server;
 typedef struct gme_server_config {
   int64_t hbm_budget_bytes; /* device memory the server may hold in all (0 = 20 GiB) */
   int64_t wave_max_cells;   /* cells per launch at most (0 = 2^35) */
   int32_t waves;            /* launch slots = launches in flight at once (0 = 4) */
   int32_t queue_max;        /* requests the host queue holds (0 = 2^20) */
-  int32_t warps_per_block;  /* batch kernel CTA shape, 4 or 8 (0 = automatic) */
-  int32_t reserved;
+  int32_t warps_per_block;  /* kernel CTA shape, 4 or 8 (0 = automatic: 4 in ring mode) */
+  int32_t mode;             /* a gme_serve_mode (0 = GME_SERVE_RING) */
 } gme_server_config;
 
 typedef struct gme_server_stats {
   int64_t submitted, completed; /* requests */
   int64_t queued, running;      /* waiting on the host; admitted to a launch */
-  int64_t waves_launched;       /* launches of the batched kernel sequence */
+  int64_t waves_launched;       /* waves mode: launches of the batched kernel sequence;
+                                 * ring mode: launches of the persistent kernel */
   int64_t kernels_launched;     /* CUDA kernels, all slots */
   int64_t cells_completed;      /* sum of n1*n2 over completed requests */
   int64_t hbm_bytes_held;       /* device memory held by the server now */
