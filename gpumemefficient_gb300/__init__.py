@@ -58,7 +58,7 @@ class BatchConfig(ctypes.Structure):
     _fields_ = [("warps_per_block", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("block_min_cells", ctypes.c_int64), ("long_min_cells", ctypes.c_int64),
                 ("team_min_cells", ctypes.c_int64), ("packed16", ctypes.c_int32),
-                ("team_split", ctypes.c_int32)]
+                ("team_split", ctypes.c_int32), ("rows_per_lane", ctypes.c_int32)]
 
 
 PAIR_DTYPE = np.dtype([("a_off", "<i8"), ("b_off", "<i8"), ("n1", "<i4"), ("n2", "<i4"),
@@ -250,9 +250,9 @@ class Context:
 
     def set_batch_config(self, warps_per_block: int = 0, blocks_per_sm: int = 0,
                          block_min_cells: int = 0, long_min_cells: int = 0, team_min_cells: int = 0,
-                         packed16: int = 0, team_split: int = 0):
+                         packed16: int = 0, team_split: int = 0, rows_per_lane: int = 0):
         cfg = BatchConfig(warps_per_block, blocks_per_sm, block_min_cells, long_min_cells, team_min_cells,
-                          int(packed16), team_split)
+                          int(packed16), team_split, rows_per_lane)
         _check(lib().gme_set_batch_config(self.handle, ctypes.byref(cfg)), self.handle)
 
     def batch_stats(self) -> dict:

@@ -425,8 +425,9 @@ gme_status gme_batch_tuned_config(const gme_pair *pairs, int64_t n, gme_batch_co
   out->block_min_cells = t.block_min_cells;
   out->long_min_cells = 0;
   out->team_min_cells = t.team_min_cells;
-  out->packed16 = 0;
+  out->packed16 = t.packed16 ? 0 : -1;
   out->team_split = t.team_split;
+  out->rows_per_lane = t.rows_per_lane;
   return GME_OK;
 }
 
@@ -498,10 +499,15 @@ gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg) {
     if (cfg->team_split) t.team_split = cfg->team_split;
     if (cfg->packed16 < -1 || cfg->packed16 > 1) return GME_ERR_INVALID;
     t.packed16 = cfg->packed16 >= 0;
+    if (cfg->rows_per_lane != 0 && cfg->rows_per_lane != 2 && cfg->rows_per_lane != 4) {
+      ctx->ws.last_error = "batch config: rows_per_lane must be 2 or 4";
+      return GME_ERR_INVALID;
+    }
+    if (cfg->rows_per_lane) t.rows_per_lane = cfg->rows_per_lane;
   }
   // an all-zero configuration means "automatic" (the tuned table)
   t.user_set = cfg && (cfg->warps_per_block || cfg->blocks_per_sm || cfg->block_min_cells ||
-                       cfg->long_min_cells || cfg->team_min_cells || cfg->team_split);
+                       cfg->long_min_cells || cfg->team_min_cells || cfg->team_split || cfg->rows_per_lane);
   if (!t.user_set && cfg) t.packed16 = cfg->packed16 >= 0;
   ctx->batch_tune = t;
   return GME_OK;

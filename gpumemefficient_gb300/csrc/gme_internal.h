@@ -62,8 +62,10 @@ struct BatchTuning {
   long long team_min_cells = 1ll << 25;
   // a team job of G band groups runs on clamp(G / team_split, 2, 8) CTAs
   int team_split = 2;
-  // pairs whose values fit 16 bits run on the packed 16-bit engine
+  // pairs whose values fit 16 bits run on the packed 16-bit engine (rows_per_lane 4 only)
   bool packed16 = true;
+  // rows per lane of the kernel: 4 (128-row bands) or 2 (64-row bands)
+  int rows_per_lane = 4;
   // false: the plan takes warps, CTAs per SM and cut-offs from the tuned table
   // (gme_tuned.h) for the batch's length bucket
   bool user_set = false;
@@ -96,7 +98,7 @@ struct BatchArena {
   long long last_block_jobs = 0, last_warp_jobs = 0, last_long_jobs = 0;
   // the plan
   long long nseg = 0;
-  int n_b = 0, n_w = 0, NW = 4, grid = 0;
+  int n_b = 0, n_w = 0, NW = 4, R = 4, grid = 0;
   int kb[4] = {0, 0, 0, 0}, kw[4] = {0, 0, 0, 0};  // per-kind offsets into the two queues
   std::vector<int> longj;             // result slots of pairs for the plain path
   std::vector<gme_pair> long_pairs;   // their descriptors
@@ -110,11 +112,11 @@ struct BatchArena {
 };
 
 // batched path (gme_batch.cu)
-bool batch_config_valid(int NW);
-int batch_occupancy(int NW);
+bool batch_config_valid(int NW, int R = 4);
+int batch_occupancy(int NW, int R = 4);
 constexpr int BATCH_MAX_N1 = 16384;  // widest pair the batch kernel takes (wider: plain path)
 long long batch_pair_bytes(long long n1, long long n2);
-long long batch_grid(int sms, int NW, int blocks_per_sm);
+long long batch_grid(int sms, int NW, int blocks_per_sm, int R = 4);
 long long batch_scratch_bytes(long long grid, int NW, int max_n1);
 // the tuned table's entry for a batch of pairs (given.user_set: `given` itself)
 BatchTuning batch_tuning_for(const gme_pair *pairs, long long npairs, const BatchTuning &given);

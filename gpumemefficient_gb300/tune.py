@@ -7,6 +7,8 @@ batched work-queue kernel:
 * CTAs per SM,
 * block_min_cells (pairs at least this large run one per CTA, the rest one per warp),
 * team_min_cells (pairs at least this large run on a team of CTAs),
+* the tile height: rows per lane (4: 128-row bands, or 2: 64-row bands),
+* the engine: packed 16-bit cells where values fit (at 4 rows per lane), or int32 only,
 
 on seeded synthetic batches whose lengths are log-uniform within the bucket (LCS,
 ED and SW one third each), timing CUDA-graph replays of one planned launch with CUDA
@@ -54,6 +56,8 @@ GRID = {
     "block_min_cells": [1 << 20, 1 << 21, 1 << 22, 1 << 23],
     "team_min_cells": [1 << 24, 1 << 25, 1 << 26, -1],
     "team_split": [2, 3, 4],
+    "rows_per_lane": [4, 2],
+    "packed16": [0, -1],   # 0: packed where values fit, -1: int32 for every pair
 }
 QUICK_GRID = {
     "warps_per_block": [4, 8],
@@ -61,7 +65,17 @@ QUICK_GRID = {
     "block_min_cells": [1 << 21, 1 << 22],
     "team_min_cells": [1 << 25, -1],
     "team_split": [2],
+    "rows_per_lane": [4, 2],
+    "packed16": [0, -1],
 }
+
+
+def redundant(cfg, grid) -> bool:
+    """Configurations that repeat another: without teams the split changes nothing; at
+    2 rows per lane there is no packed engine."""
+    if cfg.get("team_min_cells") == -1 and cfg.get("team_split", 2) != grid.get("team_split", [2])[0]:
+        return True
+    return cfg.get("rows_per_lane", 4) == 2 and cfg.get("packed16", 0) != -1
 
 
 def lengths_for(lo: int, hi: int, cells: float, rng):
@@ -141,8 +155,8 @@ def sweep(grid=None, cells: float = 1.5e10, reps: int = 5, device: int = 0, log=
         ref = None
         for vals in itertools.product(*(grid[k] for k in keys)):
             cfg = dict(zip(keys, vals))
-            if cfg.get("team_min_cells") == -1 and cfg.get("team_split", 2) != grid.get("team_split", [2])[0]:
-                continue  # no teams: the split changes nothing
+            if redundant(cfg, grid):
+                continue
             ms, split, res = measure(ctx, d_sym, d_res, pairs, len(symbols), cfg, reps, stream)
             ok = bool((res["status"] == 0).all())
             if ref is None:
@@ -188,14 +202,15 @@ def write_md(rows, best, path, cmd):
         lines.append(f"## {name}: lengths [{rs[0]['lo']}, {rs[0]['hi']}], {rs[0]['pairs']} pairs, "
                      f"{rs[0]['cells']:.3g} cells{rng_txt}")
         lines.append("")
-        lines.append("| warps/CTA | CTAs/SM | block_min | team_min | groups/member | ms | GCUPS | split (team/block/warp/plain) | |")
-        lines.append("|---:|---:|---:|---:|---:|---:|---:|---|---|")
+        lines.append("| warps/CTA | CTAs/SM | block_min | team_min | groups/member | rows/lane | packed16 | ms | GCUPS | split (team/block/warp/plain) | |")
+        lines.append("|---:|---:|---:|---:|---:|---:|---|---:|---:|---|---|")
         for r in sorted(rs, key=lambda r: -r["gcups"]):
             s = r["split"]
             mark = "best" if r == w else ("" if r["ok"] else "MISMATCH")
             lines.append(f"| {r['warps_per_block']} | {r['blocks_per_sm'] or 'max'} | 2^{int(np.log2(r['block_min_cells']))} | "
                          f"{('2^%d' % int(np.log2(r['team_min_cells']))) if r['team_min_cells'] > 0 else 'none'} | "
-                         f"{r.get('team_split', 2)} | {r['ms']:.3f} | {r['gcups']:.1f} | {s.get('team_jobs', 0)}/{s['block_jobs']}/{s['warp_jobs']}/{s['long_jobs']} | {mark} |")
+                         f"{r.get('team_split', 2)} | {r.get('rows_per_lane', 4)} | {'off' if r.get('packed16', 0) < 0 else 'on'} | "
+                         f"{r['ms']:.3f} | {r['gcups']:.1f} | {s.get('team_jobs', 0)}/{s['block_jobs']}/{s['warp_jobs']}/{s['long_jobs']} | {mark} |")
         lines.append("")
     with open(path, "w") as f:
         f.write("\n".join(lines))
@@ -213,7 +228,9 @@ def gen_header(best, path=TUNED_H, cells: float = 1.5e10):
            "// tuned on -- unless the caller set its own.",
            "#pragma once", "", "namespace gme {", "",
            "struct TunedBucket {", "  float lo, hi;", "  int warps_per_block, blocks_per_sm;",
-           "  long long block_min_cells, team_min_cells;", "  int team_split;", "};", "",
+           "  long long block_min_cells, team_min_cells;", "  int team_split;",
+           "  int rows_per_lane;  // 4 or 2", "  int packed16;       // 1: packed 16-bit cells where values fit",
+           "};", "",
            f"constexpr int TUNED_BUCKETS = {len(keys)};",
            "constexpr TunedBucket TUNED[TUNED_BUCKETS > 0 ? TUNED_BUCKETS : 1] = {"]
     for bi, (name, lo, hi) in enumerate(BUCKETS + MIXES):
@@ -222,9 +239,10 @@ def gen_header(best, path=TUNED_H, cells: float = 1.5e10):
         r = best[name]
         p_lo, p_hi = (r["p_lo"], r["p_hi"]) if "p_lo" in r else bucket_range(lo, hi, cells, 0x5EED + bi)
         out.append(f"    {{{p_lo:.1f}f, {p_hi:.1f}f, {r['warps_per_block']}, {r['blocks_per_sm']}, {r['block_min_cells']}ll, "
-                   f"{r['team_min_cells']}ll, {r.get('team_split', 2)}}},  // {name}: {r['gcups']:.0f} GCUPS")
+                   f"{r['team_min_cells']}ll, {r.get('team_split', 2)}, {r.get('rows_per_lane', 4)}, "
+                   f"{0 if r.get('packed16', 0) < 0 else 1}}},  // {name}: {r['gcups']:.0f} GCUPS")
     if not keys:
-        out.append("    {1.0f, 1.0f, 4, 0, 1ll << 22, 1ll << 25, 2},")
+        out.append("    {1.0f, 1.0f, 4, 0, 1ll << 22, 1ll << 25, 2, 4, 1},")
     out += ["};", "", "}  // namespace gme", ""]
     with open(path, "w") as f:
         f.write("\n".join(out))

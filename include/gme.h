@@ -148,13 +148,16 @@ typedef struct gme_batch_config {
                             * DPX (the default); -1: int32 for every pair */
   int32_t team_split;      /* groups of bands per team member: a team job of G groups runs
                             * on clamp(G / team_split, 2, 8) CTAs (0 = 2) */
+  int32_t rows_per_lane;   /* rows of a band per lane: 4 (128-row bands; the default) or 2
+                            * (64-row bands: more bands, shorter per-step chains); the
+                            * packed 16-bit engine runs only at 4 */
 } gme_batch_config;
 
 gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg);
 /* The settings a batch of these pairs is planned with when no configuration was set:
  * the entry of the autotuned table whose length range (2nd..98th percentile of
  * sqrt(n1*n2)) is nearest the batch's, in log scale.  Host only, needs no GPU.
- * long_min_cells is 0 (automatic) and packed16 is 0 (on) in the result. */
+ * long_min_cells is 0 (automatic); packed16 is 0 (on) or -1 (off), as the entry says. */
 gme_status gme_batch_tuned_config(const gme_pair *pairs, int64_t n, gme_batch_config *out);
 /* Host buffers; blocks until all results are in `results`. */
 gme_status gme_align_batch(gme_context *ctx, const int32_t *symbols, int64_t nsym,

@@ -21,8 +21,9 @@ def check_batch(ctx, kinds, sa, sb, rule=0, sc=None):
     return res
 
 
-@pytest.mark.parametrize("nw,packed16", [(4, -1), (8, -1), (4, 1), (8, 1)])
-def test_mixed_uneven(gme_ctx, nw, packed16):
+@pytest.mark.parametrize("nw,packed16,rows", [(4, -1, 4), (8, -1, 4), (4, 1, 4), (8, 1, 4), (4, -1, 2),
+                                              (8, -1, 2), (4, 1, 2)])
+def test_mixed_uneven(gme_ctx, nw, packed16, rows):
     rng = np.random.default_rng(31 + nw)
     n = 600
     kinds = rng.integers(0, 3, n)
@@ -30,7 +31,8 @@ def test_mixed_uneven(gme_ctx, nw, packed16):
     lb = np.exp(rng.uniform(np.log(1), np.log(3000), n)).astype(int)
     sa = [rng.integers(0, 4, k) for k in la]
     sb = [rng.integers(0, 4, k) for k in lb]
-    gme_ctx.set_batch_config(warps_per_block=nw, block_min_cells=1 << 18, packed16=packed16)
+    # at 2 rows per lane the packed engine does not exist: packed16=1 runs int32
+    gme_ctx.set_batch_config(warps_per_block=nw, block_min_cells=1 << 18, packed16=packed16, rows_per_lane=rows)
     try:
         check_batch(gme_ctx, kinds, sa, sb, rule=0)
         check_batch(gme_ctx, kinds, sa, sb, rule=1)
@@ -56,8 +58,8 @@ def test_shapes_edges(gme_ctx):
     assert st["long_jobs"] > 0
 
 
-@pytest.mark.parametrize("nw", [4, 8])
-def test_wide_pairs(gme_ctx, nw):
+@pytest.mark.parametrize("nw,rows", [(4, 4), (8, 4), (4, 2)])
+def test_wide_pairs(gme_ctx, nw, rows):
     """Rows of 4097..16384 columns: block jobs (tagged wrap rows in global memory) and warp jobs."""
     rng = np.random.default_rng(101 + nw)
     n = 60
@@ -66,7 +68,7 @@ def test_wide_pairs(gme_ctx, nw):
     lb = np.exp(rng.uniform(np.log(1), np.log(3000), n)).astype(int)
     sa = [rng.integers(0, 4, k) for k in la]
     sb = [rng.integers(0, 4, k) for k in lb]
-    gme_ctx.set_batch_config(warps_per_block=nw, block_min_cells=1 << 20)
+    gme_ctx.set_batch_config(warps_per_block=nw, block_min_cells=1 << 20, rows_per_lane=rows)
     try:
         for _ in range(2):  # the second run reuses the wrap rows with newer tags
             check_batch(gme_ctx, kinds, sa, sb, rule=0)
@@ -76,8 +78,8 @@ def test_wide_pairs(gme_ctx, nw):
         gme_ctx.set_batch_config()
 
 
-@pytest.mark.parametrize("nw,split", [(4, 2), (8, 2), (4, 3), (4, 1)])
-def test_team_jobs(gme_ctx, nw, split):
+@pytest.mark.parametrize("nw,split,rows", [(4, 2, 4), (8, 2, 4), (4, 3, 4), (4, 1, 4), (4, 2, 2), (8, 3, 2)])
+def test_team_jobs(gme_ctx, nw, split, rows):
     """Pairs shared by teams of CTAs (every T-th band group per CTA, rows handed over
     through global tagged rows, T = groups / split in 2..8); SW maxima with ties
     combined across the team."""
@@ -105,7 +107,8 @@ def test_team_jobs(gme_ctx, nw, split):
         sa.append(rng.integers(0, 4, int(rng.integers(1, 3000))))
         sb.append(rng.integers(0, 4, int(rng.integers(1, 3000))))
     gme_ctx.set_batch_config(warps_per_block=nw, team_min_cells=1 << 18, long_min_cells=-1,
-                             block_min_cells=1 << 20, packed16=1 if nw == 4 else -1, team_split=split)
+                             block_min_cells=1 << 20, packed16=1 if nw == 4 else -1, team_split=split,
+                             rows_per_lane=rows)
     try:
         for _ in range(2):
             check_batch(gme_ctx, kinds, sa, sb, rule=1)

@@ -10,7 +10,9 @@ import pytest
 from conftest import REPO
 
 BEST = json.load(open(os.path.join(REPO, "gpumemefficient_gb300", "tuned.json")))["best"]
-KEYS = ("warps_per_block", "blocks_per_sm", "block_min_cells", "team_min_cells", "team_split")
+KEYS = ("warps_per_block", "blocks_per_sm", "block_min_cells", "team_min_cells", "team_split", "rows_per_lane",
+        "packed16")
+DEFAULTS = {"team_split": 2, "rows_per_lane": 4, "packed16": 0}
 
 
 def _pairs(la, lb):
@@ -30,7 +32,7 @@ def _selected(la, lb):
 
 
 def _entry(name):
-    return {k: BEST[name].get(k, 2 if k == "team_split" else None) for k in KEYS}
+    return {k: BEST[name].get(k, DEFAULTS.get(k)) for k in KEYS}
 
 
 def test_header_is_the_committed_sweep(tmp_path):
