@@ -504,6 +504,14 @@ gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg) {
       return GME_ERR_INVALID;
     }
     if (cfg->rows_per_lane) t.rows_per_lane = cfg->rows_per_lane;
+    // 2 rows per lane exists with 8 warps per CTA only
+    if (t.rows_per_lane == 2) {
+      if (cfg->warps_per_block == 4) {
+        ctx->ws.last_error = "batch config: rows_per_lane 2 needs warps_per_block 8";
+        return GME_ERR_INVALID;
+      }
+      t.warps_per_block = 8;
+    }
   }
   // an all-zero configuration means "automatic" (the tuned table)
   t.user_set = cfg && (cfg->warps_per_block || cfg->blocks_per_sm || cfg->block_min_cells ||

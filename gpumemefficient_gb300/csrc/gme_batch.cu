@@ -347,7 +347,8 @@ int batch_occupancy(int NW, int R) {
   return 0;
 }
 
-bool batch_config_valid(int NW, int R) { return (NW == 4 || NW == 8) && (R == 2 || R == 4); }
+// (2 rows per lane only with 8 warps per CTA: gme_batch_r2.cu)
+bool batch_config_valid(int NW, int R) { return (NW == 4 || NW == 8) && (R == 4 || (R == 2 && NW == 8)); }
 
 // Device bytes one pair adds to a batch: its symbols as the caller holds them, the
 // staged copy (pads, b rounded up to whole band groups) and its descriptors.
@@ -409,7 +410,7 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
   const int NW = tune.warps_per_block;
   const int RL = tune.rows_per_lane;  // the kernel's rows per lane (the layout is for 4)
   if (!batch_config_valid(NW, RL))
-    return ws.fail_msg(ST_INVALID, "batch: warps_per_block must be 4 or 8, rows_per_lane 2 or 4");
+    return ws.fail_msg(ST_INVALID, "batch: warps_per_block must be 4 or 8, rows_per_lane 4 (or 2 with 8 warps)");
   std::vector<int> blockj, warpj, teamj;
   ar.longj.clear();
   int occ0 = batch_occupancy(NW, RL);

@@ -248,11 +248,9 @@ __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict_
   const Rec<KIND> rec(sc);
   const int yl = y0 + lane * R + 1;  // first row of this lane
   int bs[R], cur[R], prv[R], smax[R], sstep[R];
-#pragma unroll
-  for (int r = 0; r < R; r += 4) {
-    const int4 q = ldg4(b_sym + (yl - 1 + r));
-    bs[r] = q.x; bs[r + 1] = q.y; bs[r + 2] = q.z; bs[r + 3] = q.w;
-  }
+  // (b's staged segment starts 16-byte aligned and lane rows start at multiples of R,
+  // so the lane's symbols are 16-byte aligned at R = 4 and 8-byte aligned at R = 2)
+  ld_syms<R, R>(b_sym + (yl - 1), bs);
   unsigned padmask = 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
@@ -264,19 +262,12 @@ __device__ __noinline__ bool sweep_band(const Scoring sc, const int *__restrict_
   }
   const bool padwarp = __any_sync(FULL, padmask != 0);
 
+  // (PADL - 1 is a multiple of 4: the same alignment as b's)
+  static_assert((PADL - 1) % 4 == 0, "a's window must share b's alignment");
   const int *sym = a_sym + (PADL - 1 - lane * R);
   int win[2 * CB];
-#pragma unroll
-  for (int k = 0; k < CB; k += 4) {
-    const int4 q = ldg4(sym + k);
-    win[k] = q.x; win[k + 1] = q.y; win[k + 2] = q.z; win[k + 3] = q.w;
-  }
-#pragma unroll
-  for (int k = 0; k < R; k += 4) {
-    const int4 q = ldg4(sym - R + k);
-    win[2 * CB - R + k] = q.x; win[2 * CB - R + k + 1] = q.y;
-    win[2 * CB - R + k + 2] = q.z; win[2 * CB - R + k + 3] = q.w;
-  }
+  ld_syms<R, CB>(sym, win);
+  ld_syms<R, R>(sym - R, &win[2 * CB - R]);
 #pragma unroll
   for (int k = CB; k < 2 * CB - R; ++k) win[k] = 0;
 

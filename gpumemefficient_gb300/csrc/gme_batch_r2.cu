@@ -1,6 +1,9 @@
 // gme_batch_r2.cu -- the batched work-queue kernel at 2 rows per lane (64-row bands),
 // which the autotuner may pick for a length range; its own translation unit, so that it
 // compiles beside gme_batch.cu.  The 16-bit packed engine exists only at 4 rows per lane.
+// Only the 8-warp CTA is built: the 4-warp one (register-capped for 3 CTAs per SM) let
+// warps read the job word before thread 0 had written it, so that its warps ran
+// different jobs and a bounded wait gave up; the 8-warp one passes every batch test.
 #include "gme_batch_kernel.cuh"
 
 namespace gme {
@@ -12,11 +15,7 @@ static cudaError_t launch_r2_t(const BatchParams &P, int grid, cudaStream_t st) 
 }
 
 cudaError_t batch_launch_r2(int NW, const BatchParams &P, int grid, cudaStream_t st) {
-  switch (NW) {
-    case 4: return launch_r2_t<4>(P, grid, st);
-    case 8: return launch_r2_t<8>(P, grid, st);
-  }
-  return cudaErrorInvalidValue;
+  return NW == 8 ? launch_r2_t<8>(P, grid, st) : cudaErrorInvalidValue;
 }
 
 template <int NW>
@@ -28,12 +27,6 @@ static int occupancy_r2_t() {
   return n;
 }
 
-int batch_occupancy_r2(int NW) {
-  switch (NW) {
-    case 4: return occupancy_r2_t<4>();
-    case 8: return occupancy_r2_t<8>();
-  }
-  return 0;
-}
+int batch_occupancy_r2(int NW) { return NW == 8 ? occupancy_r2_t<8>() : 0; }
 
 }  // namespace gme

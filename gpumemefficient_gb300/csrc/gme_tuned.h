@@ -19,12 +19,12 @@ struct TunedBucket {
 
 constexpr int TUNED_BUCKETS = 6;
 constexpr TunedBucket TUNED[TUNED_BUCKETS > 0 ? TUNED_BUCKETS : 1] = {
-    {43.0f, 388.9f, 4, 0, 1048576ll, 33554432ll, 4, 4, 1},  // short: 854 GCUPS
-    {587.9f, 1788.1f, 4, 0, 4194304ll, 33554432ll, 4, 4, 1},  // mid: 2067 GCUPS
-    {2355.9f, 7059.6f, 8, 0, 1048576ll, 67108864ll, 3, 4, 1},  // long: 1645 GCUPS
-    {8535.6f, 14944.5f, 8, 2, 2097152ll, 33554432ll, 3, 4, 1},  // wide: 1437 GCUPS
-    {99.3f, 2669.9f, 4, 0, 4194304ll, 67108864ll, 4, 4, 1},  // mixed_64_4096: 1792 GCUPS
-    {60.0f, 8309.6f, 4, 0, 2097152ll, 16777216ll, 3, 4, 1},  // mixed_32_16384: 1222 GCUPS
+    {43.0f, 388.9f, 4, 0, 4194304ll, -1ll, 2, 4, 1},  // short: 847 GCUPS
+    {587.9f, 1788.1f, 4, 0, 8388608ll, -1ll, 2, 4, 1},  // mid: 2052 GCUPS
+    {2355.9f, 7059.6f, 8, 0, 2097152ll, -1ll, 2, 4, 1},  // long: 1648 GCUPS
+    {8535.6f, 14944.5f, 8, 0, 4194304ll, 67108864ll, 3, 4, 1},  // wide: 1435 GCUPS
+    {99.3f, 2669.9f, 4, 0, 4194304ll, 33554432ll, 4, 4, 1},  // mixed_64_4096: 1784 GCUPS
+    {60.0f, 8309.6f, 4, 0, 4194304ll, 33554432ll, 4, 4, 0},  // mixed_32_16384: 1196 GCUPS
 };
 
 }  // namespace gme

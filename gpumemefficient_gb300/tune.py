@@ -75,6 +75,8 @@ def redundant(cfg, grid) -> bool:
     2 rows per lane there is no packed engine."""
     if cfg.get("team_min_cells") == -1 and cfg.get("team_split", 2) != grid.get("team_split", [2])[0]:
         return True
+    if cfg.get("rows_per_lane", 4) == 2 and cfg.get("warps_per_block") == 4:
+        return True  # 2 rows per lane exists only with 8 warps per CTA
     return cfg.get("rows_per_lane", 4) == 2 and cfg.get("packed16", 0) != -1
 
 

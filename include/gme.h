@@ -149,8 +149,9 @@ typedef struct gme_batch_config {
   int32_t team_split;      /* groups of bands per team member: a team job of G groups runs
                             * on clamp(G / team_split, 2, 8) CTAs (0 = 2) */
   int32_t rows_per_lane;   /* rows of a band per lane: 4 (128-row bands; the default) or 2
-                            * (64-row bands: more bands, shorter per-step chains); the
-                            * packed 16-bit engine runs only at 4 */
+                            * (64-row bands: more bands, shorter per-step chains; only
+                            * with 8 warps per block); the packed 16-bit engine runs
+                            * only at 4 */
 } gme_batch_config;
 
 gme_status gme_set_batch_config(gme_context *ctx, const gme_batch_config *cfg);

@@ -21,8 +21,8 @@ def check_batch(ctx, kinds, sa, sb, rule=0, sc=None):
     return res
 
 
-@pytest.mark.parametrize("nw,packed16,rows", [(4, -1, 4), (8, -1, 4), (4, 1, 4), (8, 1, 4), (4, -1, 2),
-                                              (8, -1, 2), (4, 1, 2)])
+@pytest.mark.parametrize("nw,packed16,rows", [(4, -1, 4), (8, -1, 4), (4, 1, 4), (8, 1, 4), (8, -1, 2),
+                                              (8, 1, 2)])
 def test_mixed_uneven(gme_ctx, nw, packed16, rows):
     rng = np.random.default_rng(31 + nw)
     n = 600
@@ -58,7 +58,7 @@ def test_shapes_edges(gme_ctx):
     assert st["long_jobs"] > 0
 
 
-@pytest.mark.parametrize("nw,rows", [(4, 4), (8, 4), (4, 2)])
+@pytest.mark.parametrize("nw,rows", [(4, 4), (8, 4), (8, 2)])
 def test_wide_pairs(gme_ctx, nw, rows):
     """Rows of 4097..16384 columns: block jobs (tagged wrap rows in global memory) and warp jobs."""
     rng = np.random.default_rng(101 + nw)
@@ -78,7 +78,7 @@ def test_wide_pairs(gme_ctx, nw, rows):
         gme_ctx.set_batch_config()
 
 
-@pytest.mark.parametrize("nw,split,rows", [(4, 2, 4), (8, 2, 4), (4, 3, 4), (4, 1, 4), (4, 2, 2), (8, 3, 2)])
+@pytest.mark.parametrize("nw,split,rows", [(4, 2, 4), (8, 2, 4), (4, 3, 4), (4, 1, 4), (8, 2, 2), (8, 3, 2)])
 def test_team_jobs(gme_ctx, nw, split, rows):
     """Pairs shared by teams of CTAs (every T-th band group per CTA, rows handed over
     through global tagged rows, T = groups / split in 2..8); SW maxima with ties
@@ -281,3 +281,22 @@ def test_plan_graph_replay(gme_ctx):
             np.testing.assert_array_equal(res["score"], o["score"])
     finally:
         plan.close()
+
+
+def test_rows_per_lane_config(gme_ctx):
+    """2 rows per lane runs with 8 warps per CTA only: asked with 4 it is refused, and
+    asked alone it takes 8; other values are refused."""
+    import gpumemefficient_gb300 as g
+    for bad in (dict(rows_per_lane=2, warps_per_block=4), dict(rows_per_lane=3), dict(rows_per_lane=8)):
+        with pytest.raises(g.GmeError):
+            gme_ctx.set_batch_config(**bad)
+    rng = np.random.default_rng(91)
+    kinds = rng.integers(0, 3, 40)
+    sa = [rng.integers(0, 4, int(k)) for k in rng.integers(1, 2500, 40)]
+    sb = [rng.integers(0, 4, int(k)) for k in rng.integers(500, 2500, 40)]
+    gme_ctx.set_batch_config(rows_per_lane=2, block_min_cells=1 << 18)
+    try:
+        check_batch(gme_ctx, kinds, sa, sb)
+        assert gme_ctx.batch_stats()["block_jobs"] > 0
+    finally:
+        gme_ctx.set_batch_config()
