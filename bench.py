@@ -466,6 +466,49 @@ def run_gme_batch(args):
     plain_gcups = float(cells_k[sub].sum()) / (e0.elapsed_time(e1) / 1e3) / 1e9
     del offs
 
+    # what batching buys where one pair alone already fills part of the GPU: 64 pairs
+    # with lengths log-uniform in [2048, 4096], one planned launch against one plain
+    # call per pair (both on resident inputs, CUDA events)
+    lrng = np.random.default_rng(synth.SEED_BATCH + 7)
+    lk = lrng.integers(0, 3, 64)
+    la = np.exp(lrng.uniform(np.log(2048), np.log(4096), 64)).astype(int)
+    lb = np.exp(lrng.uniform(np.log(2048), np.log(4096), 64)).astype(int)
+    lsa = [lrng.integers(0, 4, int(x)).astype(np.int32) for x in la]
+    lsb = [lrng.integers(0, 4, int(x)).astype(np.int32) for x in lb]
+    lsym, lpairs = g.pack_batch(lk, lsa, lsb)
+    lcells = float((la.astype(np.float64) * lb).sum())
+    with torch.cuda.stream(stream):
+        ld_sym = torch.from_numpy(lsym).to(dev)
+        ld_res = torch.zeros(64 * g.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    lplan = g.BatchPlan(ctx, lpairs, len(lsym))
+    for _ in range(3):
+        lplan.run(ld_sym.data_ptr(), ld_res.data_ptr(), stream=sp, use_graph=True)
+    e0.record(stream)
+    for _ in range(10):
+        lplan.run(ld_sym.data_ptr(), ld_res.data_ptr(), stream=sp, use_graph=True)
+    e1.record(stream)
+    stream.synchronize()
+    large_batched = lcells * 10 / (e0.elapsed_time(e1) / 1e3) / 1e9
+    lres = np.frombuffer(ld_res.cpu().numpy().tobytes(), g.RESULT_DTYPE)
+    large_ok = bool((lres["score"] == O.align_batch(lk, lsa, lsb, threads=os.cpu_count() or 1)["score"]).all())
+    lplan.close()
+
+    def _plain_all():
+        for i in range(64):
+            ctx.align_device(int(lk[i]), ld_sym.data_ptr() + 4 * int(lpairs[i]["a_off"]), int(lpairs[i]["n1"]),
+                             ld_sym.data_ptr() + 4 * int(lpairs[i]["b_off"]), int(lpairs[i]["n2"]),
+                             d_one.data_ptr(), stream=sp)
+    _plain_all()
+    stream.synchronize()
+    e0.record(stream)
+    _plain_all()
+    e1.record(stream)
+    stream.synchronize()
+    large_plain = lcells / (e0.elapsed_time(e1) / 1e3) / 1e9
+    large = {"pairs": 64, "lengths": "log-uniform [2048, 4096], LCS/ED/SW mixed", "cells": lcells,
+             "batched_gcups": large_batched, "plain_per_pair_gcups": large_plain,
+             "batched_over_plain": large_batched / large_plain, "parity_vs_oracle": "ok" if large_ok else "MISMATCH"}
+
     props = torch.cuda.get_device_properties(local)
     sms = props.multi_processor_count
     mhz = clk.get("sm_mhz") or 1920.0
@@ -492,7 +535,7 @@ def run_gme_batch(args):
            "pairs": n, "cells": cells, "seed": synth.SEED_BATCH, "split": split,
            "l2": "flushed between timed steps (256 MiB write)", "parity_vs_oracle": "ok" if parity else "MISMATCH",
            "plain_per_pair_gcups": plain_gcups, "plain_sample_pairs": int(len(sub)),
-           "batched_over_plain": value / ws / plain_gcups}
+           "batched_over_plain": value / ws / plain_gcups, "large_pairs": large}
     line = {"metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * mean_s,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -767,7 +810,9 @@ def run_gme_sat(args):
     import gpumemefficient_gb300 as g
     from oracle import oracle as O
     n1 = n2 = args.sat_n
-    ld = n1 + 3
+    # the reference's layout (rows of n1 + 3 ints), or rows rounded up to 16 bytes, which
+    # takes the tensor-map kernel
+    ld = n1 + 3 if args.sat_layout == "reference" else (n1 + 3 + 3) // 4 * 4
     rng = np.random.default_rng(0x5A7)
     host = rng.integers(0, 10000, (n2 + 2, ld), dtype=np.int32)
     cells = n1 * n2
@@ -825,11 +870,14 @@ def run_gme_sat(args):
         peak, basis = 6800.0, "fallback 6.8 TB/s"
     achieved = 8.0 * cells / t / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": profiled_traffic("sat_kernel_16384"), "peak_basis": basis,
-            "bytes_per_cell": 8, "kernel": "sat_kernel (one launch)"}
+            "traffic": profiled_traffic("sat_kernel_16384" if ld % 4 else "sat_tma_kernel_16384"),
+            "peak_basis": basis, "bytes_per_cell": 8,
+            "kernel": ("sat_kernel" if ld % 4 else "sat_tma_kernel (tensor maps)") + " (one launch)"}
     cpu = sat_cpu_baseline(host, n1, n2, ld) if rank == 0 and not args.no_cpu else None
-    cfg = {"workload": f"summed-area table, {n1} x {n2} interior in the reference's layout "
+    layout = "the reference's layout" if ld == n1 + 3 else "rows padded to 16 bytes"
+    cfg = {"workload": f"summed-area table, {n1} x {n2} interior in {layout} "
                        f"({n2 + 2} rows of {ld} ints, values 0..9999 seeded), in place, one launch",
+           "layout": args.sat_layout,
            "n1": n1, "n2": n2, "ld": ld, "seed": 0x5A7,
            "l2": "table (4.3 GB at 32768) larger than L2; input restored and L2 flushed (256 MiB write) before each step",
            "parity_vs_oracle": "ok" if parity and ok_status else "MISMATCH"}
@@ -883,6 +931,8 @@ def main():
     p.add_argument("--rate-seconds", type=float, default=2.0, help="served workload: seconds per rate point")
     p.add_argument("--wave-cells", type=int, default=0, help="served workload: cells per launch at most (0 = default)")
     p.add_argument("--no-parity", action="store_true", help="skip the oracle parity check (tuning runs)")
+    p.add_argument("--sat-layout", choices=["reference", "aligned"], default="reference",
+                   help="sat workload: rows of n1 + 3 ints (the reference's), or rounded up to 16 bytes")
     p.add_argument("--sat-n", type=int, default=32768,
                    help="sat workload: interior side (the reference's `15 15` case is 32768)")
     p.add_argument("--solo", action="store_true",
@@ -938,7 +988,8 @@ def also_batched_served(args):
     out["batched"] = {"workload": c["workload"], "value": b["value"], "unit": "GCUPS",
                       "ms_per_step": b["ms_per_step"], "e2e": b["e2e"]["value"],
                       "plain_per_pair_gcups": c["plain_per_pair_gcups"],
-                      "batched_over_plain": c["batched_over_plain"], "split": c["split"],
+                      "batched_over_plain": c["batched_over_plain"], "large_pairs": c["large_pairs"],
+                      "split": c["split"],
                       "parity_vs_oracle": c["parity_vs_oracle"], "roofline_frac": b["roofline"]["frac"],
                       "gpu_launches": b["gpu_launches"], "clocks": b["clocks"]}
     a = copy.copy(args)
@@ -952,19 +1003,21 @@ def also_batched_served(args):
                      "parity_vs_oracle": c["parity_vs_oracle"], "hbm_bytes_peak": c["hbm_bytes_peak"],
                      "hbm_budget_bytes": c["hbm_budget_bytes"], "gpu_launches": s["gpu_launches"],
                      "clocks": s["clocks"]}
-    # last: it sets its own stream as the current one
-    a = copy.copy(args)
-    a.steps, a.warmup, a.no_cpu, a.sat_n = 10, 3, True, 32768
-    try:
-        t = run_gme_sat(a)
-        c = t["config"]
-        out["sat"] = {"workload": c["workload"], "value": t["value"], "unit": "GCUPS",
-                      "ms_per_step": t["ms_per_step"], "e2e": t["e2e"]["value"],
-                      "roofline": {k: t["roofline"][k] for k in ("bound", "achieved", "peak", "unit", "frac")},
-                      "parity_vs_oracle": c["parity_vs_oracle"], "gpu_launches": t["gpu_launches"],
-                      "clocks": t["clocks"]}
-    except Exception as e:  # the headline line stands on its own
-        out["sat"] = {"error": repr(e)[:300]}
+    # last: it sets its own stream as the current one; the reference's layout (cp.async
+    # kernel), then rows padded to 16 bytes (tensor-map kernel)
+    for key, layout in (("sat", "reference"), ("sat_aligned", "aligned")):
+        a = copy.copy(args)
+        a.steps, a.warmup, a.no_cpu, a.sat_n, a.sat_layout = 10, 3, True, 32768, layout
+        try:
+            t = run_gme_sat(a)
+            c = t["config"]
+            out[key] = {"workload": c["workload"], "value": t["value"], "unit": "GCUPS",
+                        "ms_per_step": t["ms_per_step"], "e2e": t["e2e"]["value"],
+                        "roofline": {k: t["roofline"][k] for k in ("bound", "achieved", "peak", "unit", "frac", "kernel")},
+                        "parity_vs_oracle": c["parity_vs_oracle"], "gpu_launches": t["gpu_launches"],
+                        "clocks": t["clocks"]}
+        except Exception as e:  # the headline line stands on its own
+            out[key] = {"error": repr(e)[:300]}
     return out
 
 

@@ -122,3 +122,66 @@ def test_sat_tags_never_pass_for_band_rows():
             o = O.align(O.ED, a, b, threads=threads)
             assert r.score == o["score"], i
             np.testing.assert_array_equal(r.last_row, o["last_row"])
+
+
+TMA_SHAPES = [(1, 1, 4), (3, 5, 4), (127, 31, 128), (128, 32, 132), (129, 33, 132), (255, 64, 256),
+              (256, 65, 260), (1000, 100, 1004), (4095, 97, 4096), (4096, 130, 4100), (70, 3000, 72),
+              (5000, 300, 5004), (777, 161, 1024), (33, 64, 512)]
+
+
+@pytest.mark.parametrize("n1,n2,ld", TMA_SHAPES)
+def test_sat_tensor_map_path(gme_ctx, n1, n2, ld):
+    """Rows of a multiple of 16 bytes take the tensor-map kernel (strips from column 0,
+    boxes of 32 x 32 with 128-byte swizzle): ragged edges in both directions, padding
+    columns and the extra rows past n2 come back as they were, values wrap."""
+    import torch
+    assert ld % 4 == 0
+    rng = np.random.default_rng(n1 * 31 + n2 * 7 + ld)
+    t = _table(rng, n1, n2, ld, full_range=True)
+    want = O.sat(t, n1, n2)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        d = torch.from_numpy(t).cuda()
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        gme_ctx.sat_device(d.data_ptr(), n1, n2, ld, st.data_ptr(), s.cuda_stream)
+        s.synchronize()
+        assert int(st.item()) == 0
+        got = d.cpu().numpy()
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(got[:, n1 + 1:], t[:, n1 + 1:])  # padding columns untouched
+    np.testing.assert_array_equal(got[n2 + 1:], t[n2 + 1:])        # rows past n2 untouched
+
+
+def test_sat_unaligned_table_takes_the_copy_kernel(gme_ctx):
+    """A table whose start is not 16-byte aligned (here 4 bytes in) runs on the cp.async
+    kernel even with 16-byte rows, with the same result."""
+    import torch
+    rng = np.random.default_rng(77)
+    n1, n2, ld = 600, 90, 604
+    t = _table(rng, n1, n2, ld, full_range=True)
+    want = O.sat(t, n1, n2)
+    d = torch.zeros(t.size + 4, dtype=torch.int32, device="cuda")
+    d[1:1 + t.size] = torch.from_numpy(t.reshape(-1)).cuda()
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    gme_ctx.sat_device(d.data_ptr() + 4, n1, n2, ld, st.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    np.testing.assert_array_equal(d[1:1 + t.size].cpu().numpy().reshape(t.shape), want)
+
+
+def test_sat_tensor_map_large_closed_form(gme_ctx):
+    """8192 x 8192 in a 16-byte-row layout (ld = n1 + 4) against the threaded oracle,
+    twice, so that the tags of a second call meet the first call's words."""
+    import torch
+    rng = np.random.default_rng(5)
+    n1 = n2 = 8192
+    ld = n1 + 4
+    t = rng.integers(0, 10000, (n2 + 2, ld)).astype(np.int32)
+    want = O.sat_mt(t, n1, n2)
+    for _ in range(2):
+        d = torch.from_numpy(t).cuda()
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        gme_ctx.sat_device(d.data_ptr(), n1, n2, ld, st.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        assert int(st.item()) == 0
+        np.testing.assert_array_equal(d.cpu().numpy(), want)
