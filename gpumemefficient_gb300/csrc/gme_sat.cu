@@ -13,38 +13,41 @@
 // So a CTA that owns a strip of W = 128 columns needs, for each row, a single
 // number from the strips to its left (D_y at the last column before the strip) and
 // keeps its own columns' running sums t[y-1][x] in registers.  Per block of 32 rows:
-//   1. the block's 32 x 128 values arrive in shared memory by 4-byte cp.async (any
-//      row stride), four blocks ahead of the one being computed;
+//   1. the block's 32 x 128 values arrive in shared memory;
 //   2. four lanes per row scan it serially, 32 columns each, and combine their
-//      segment totals with two shuffles; the lane holding the row total publishes
-//      it (an "aggregate" word), looks back over the strips to its left -- adding
-//      their aggregates until it meets an "inclusive" word, a strip whose carry is
+//      segment totals with shuffles; the lane holding the row total publishes it
+//      (an "aggregate" word), looks back over the strips to its left -- adding their
+//      aggregates until it meets an "inclusive" word, a strip whose carry is
 //      complete -- and publishes its own inclusive carry.  Strip 0 starts from
 //      D_y(0), formed from column 0.  This is the decoupled look-back of single-pass
 //      prefix scans (Merrill and Garland, 2016) applied along each row: no strip
 //      waits for the whole chain of strips to its left, only for their aggregates,
-//      which every strip publishes without waiting for anything.  The lanes write
-//      D_y(x) back in place;
-//   3. one lane per column walks the block's rows: t += D, stored to the table.
-// A pad word per 32 columns keeps both shared-memory patterns free of bank
-// conflicts.  Words are 64 bits: {tag, value}, one per strip and row.  Each call
-// takes two fresh tags from the context's counter, T for aggregates and T + 1 for
-// inclusive carries, stored as the word's whole high half: the same format and the
-// same counter as the plain kernel's band words, which share this scratch, so no
-// word left by one call can pass for a word of a later call of either kind and
+//      which every strip publishes without waiting for anything;
+//   3. one lane per column walks the block's rows: t += prefix + the row's offset.
+// Each step is latency-bound, so a CTA has two roles of 4 warps: the scan warps run
+// step 2 for block k (its look-back one block later, from a word requested before
+// the scan) while the column warps run step 3 for an earlier block, handing stages
+// over through mbarriers.  Words are 64 bits: {tag, value}, one per strip and row.
+// Each call takes two fresh tags from the context's counter, T for aggregates and
+// T + 1 for inclusive carries, stored as the word's whole high half: the same format
+// and the same counter as the plain kernel's band words, which share this scratch,
+// so no word left by one call can pass for a word of a later call of either kind and
 // nothing needs clearing.  The table is read and written once: 8 bytes per cell of
 // HBM traffic.
 //
-// Tables whose rows are a multiple of 16 bytes (ld % 4 == 0, the table 16-byte aligned)
-// take a second kernel, sat_tma_kernel, on a 2D tensor map: the strips are then
-// 16-byte aligned (columns 128 s .. 128 s + 127; strip 0 holds the border column 0,
-// written back unchanged), each 32 x 128 block arrives as four 32 x 32 boxes by
-// cp.async.bulk.tensor with 128-byte swizzle (one thread issues them, an mbarrier per
-// stage counts their bytes), the row scan reads 16-byte chunks of the swizzled rows
-// and the column pass single words, both without bank conflicts, and the finished
-// block leaves by four tensor stores from shared memory.  Padding columns past n1
-// are written back as they were read; rows past n2 and columns past ld lie outside
-// the map, so loads fill them with zeros and stores skip them.
+// Two kernels move the blocks.  Any row stride (the reference's n1 + 3 is odd):
+// sat_ws_kernel, the column warps loading their own columns by 4-byte cp.async into
+// rows padded by a word per 32 columns (no bank conflicts).  Rows of a multiple of
+// 16 bytes (ld % 4 == 0, the table 16-byte aligned): sat_tma_kernel on a 2D tensor
+// map: the strips are then 16-byte aligned (columns 128 s .. 128 s + 127; strip 0
+// holds the border column 0, written back unchanged), each 32 x 128 block arrives as
+// four 32 x 32 boxes by cp.async.bulk.tensor with 128-byte swizzle (one thread issues
+// them, an mbarrier per stage counts their bytes), the row scan reads 16-byte chunks
+// of the swizzled rows and the column pass single words, both without bank
+// conflicts, and the finished block leaves by four tensor stores from shared memory.
+// Padding columns past n1 are written back as they were read; rows past n2 and
+// columns past ld lie outside the map, so loads fill them with zeros and stores skip
+// them.
 #include <algorithm>
 #include <cstdint>
 
@@ -57,28 +60,13 @@ namespace gme {
 
 namespace {
 
-#ifndef GME_SAT_WIDTH
-#define GME_SAT_WIDTH 128
-#endif
-#ifndef GME_SAT_STAGES
-#define GME_SAT_STAGES 5
-#endif
-constexpr int SAT_W = GME_SAT_WIDTH;         // strip width: one column per thread (64 or 128)
-constexpr int SAT_THREADS = SAT_W;
-constexpr int SAT_SEG = SAT_W / 32;          // 32-column segments per row
-#ifndef GME_SAT_ROWS
-#define GME_SAT_ROWS 32
-#endif
-// rows per block (measured at 32768 x 32768: 64 rows with 2 or 3 stages 2.82-2.84 ms
-// against 2.57 ms for 32 rows with 5)
-constexpr int SAT_RB = GME_SAT_ROWS;
-constexpr int SAT_RPT = SAT_RB / (SAT_THREADS / SAT_SEG);  // rows per row-scan lane group
-// blocks in shared memory (measured at 32768 x 32768: 3 stages 2.76 ms, 5 stages
-// 2.58 ms; 64-column strips 2.94-2.95 ms, their carries double)
-constexpr int SAT_STAGES = GME_SAT_STAGES;
+// strip width (one column per column-pass thread) and rows per block: 128 x 32
+// (measured before the two roles, at 32768 x 32768: 64-column strips 2.94 ms, their
+// carries double; 64-row blocks 2.82 ms; 128 x 32 2.57 ms)
+constexpr int SAT_W = 128;
+constexpr int SAT_SEG = SAT_W / 32;            // 32-column segments per row
+constexpr int SAT_RB = 32;
 constexpr int SAT_PITCH = SAT_W + SAT_W / 32;  // a pad word per 32 columns
-static_assert(SAT_W == 64 || SAT_W == 128, "strip width 64 or 128");
-static_assert(SAT_RB == 32 || SAT_RB == 64, "32 or 64 rows per block");
 constexpr unsigned FULL = 0xffffffffu;
 
 struct SatParams {
@@ -92,7 +80,6 @@ struct SatParams {
   unsigned long long timeout_ns;
 };
 
-constexpr size_t SAT_SMEM = (size_t)SAT_STAGES * SAT_RB * SAT_PITCH * sizeof(int);
 
 __device__ __forceinline__ int sat_col(int c) { return c + (c >> 5); }
 
@@ -101,149 +88,9 @@ __device__ __forceinline__ void cp_async4(int *dst, const int *src, bool valid) 
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(valid ? 4 : 0)
                : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-__global__ void __launch_bounds__(SAT_THREADS) sat_kernel(SatParams P) {
-  extern __shared__ __align__(16) int sat_smem[];
-  __shared__ int s_strip, s_abort;
-  const int tid = threadIdx.x;
-  const int lane = tid & 31;
-  if (tid == 0) s_abort = 0;
-  Waiter W(P.timeout_ns, &P.ctrl[1], &s_abort);
-  const long long n1 = P.n1, n2 = P.n2, ld = P.ld;
-  const long long nblk = (n2 + SAT_RB - 1) / SAT_RB;
-  // row-scan role: row rr of the block, segment g (columns 32g .. 32g+31)
-  const int rr = tid / SAT_SEG, g = tid % SAT_SEG;
-  for (;;) {
-    __syncthreads();
-    // strips are claimed in order: the strips to the left are always held by running CTAs
-    if (tid == 0) s_strip = s_abort ? P.strips : atomicAdd(&P.ctrl[0], 1);
-    __syncthreads();
-    const int s = s_strip;
-    if (s >= P.strips) break;
-    const long long x0 = (long long)s * SAT_W;  // the strip's columns are x0 + 1 .. x0 + W
-    const long long x = x0 + 1 + tid;           // this thread's column (load and column pass)
-    const bool xok = x <= n1;
-    unsigned col = xok ? (unsigned)P.table[x] : 0u;  // row 0
-    unsigned long long *own = P.carry + (long long)s * P.cstride;
-    const bool publish = s + 1 < P.strips;
-    const unsigned tag_agg = P.tag, tag_inc = P.tag + 1u;  // the words' high halves
-    auto issue = [&](long long b) {
-      if (b < nblk) {
-        int *t = sat_smem + (int)(b % SAT_STAGES) * (SAT_RB * SAT_PITCH) + sat_col(tid);
-        const long long y0 = 1 + b * SAT_RB;
-        const int *src = P.table + y0 * ld + x;
-#pragma unroll 8
-        for (int r = 0; r < SAT_RB; ++r, src += ld) {
-          const bool ok = xok && y0 + r <= n2;
-          cp_async4(t + r * SAT_PITCH, ok ? src : P.table, ok);
-        }
-      }
-      cp_async_commit();  // one group per block (empty past the end) keeps the count uniform
-    };
-#pragma unroll
-    for (int b = 0; b < SAT_STAGES - 1; ++b) issue(b);
-    bool failed = false;
-    for (long long b = 0; b < nblk; ++b) {
-      cp_async_wait<SAT_STAGES - 2>();  // this thread's copies of block b have landed
-      __syncthreads();                  // (1) everyone's have; the stage of block b-1 is free
-      // (no abort test here: the abort word is only set inside the look-back wait,
-      // between barriers (1) and (2), and barrier (2) decides for the whole CTA)
-      issue(b + SAT_STAGES - 1);
-      int *tile = sat_smem + (int)(b % SAT_STAGES) * (SAT_RB * SAT_PITCH);
-      const long long y0 = 1 + b * SAT_RB;
-      // 2. rows rr + 32q, segment g: serial prefix, then the row's segments combined
-      unsigned pv[SAT_RPT][32], inc[SAT_RPT], seg_excl[SAT_RPT], c[SAT_RPT];
-      bool live[SAT_RPT], done[SAT_RPT];
-      long long yq[SAT_RPT], jq[SAT_RPT];
-#pragma unroll
-      for (int q = 0; q < SAT_RPT; ++q) {
-        const int *rowp = tile + (rr + 32 * q) * SAT_PITCH + 33 * g;
-        unsigned acc = 0;
-#pragma unroll
-        for (int i = 0; i < 32; ++i) { acc += (unsigned)rowp[i]; pv[q][i] = acc; }
-        unsigned t = acc;
-#pragma unroll
-        for (int d = 1; d < SAT_SEG; d <<= 1) {
-          const unsigned u = __shfl_up_sync(FULL, t, d, SAT_SEG);
-          if (g >= d) t += u;
-        }
-        inc[q] = t;
-        seg_excl[q] = t - acc;
-        // the row's last segment holds the row total (rows beyond n2 and the other
-        // lanes read nothing and always agree)
-        yq[q] = y0 + rr + 32 * q;
-        live[q] = g == SAT_SEG - 1 && yq[q] <= n2;
-        c[q] = 0;
-        done[q] = !live[q];
-        jq[q] = s - 1;
-        if (s == 0) {
-          if (live[q]) c[q] = (unsigned)P.table[yq[q] * ld] - (unsigned)P.table[(yq[q] - 1) * ld];
-        } else if (live[q] && publish) {
-          st_relaxed_gpu_u64(own + yq[q], ((unsigned long long)tag_agg << 32) | inc[q]);
-        }
-      }
-      // look back for every row of this lane at once
-      if (s > 0) {
-        const bool ok = W.wait([&] {
-#pragma unroll
-          for (int q = 0; q < SAT_RPT; ++q) {
-            if (!done[q]) {
-              const unsigned long long wv = ld_relaxed_gpu_u64(P.carry + jq[q] * P.cstride + yq[q]);
-              const unsigned hi = (unsigned)(wv >> 32);
-              if (hi == tag_inc) {
-                c[q] += (unsigned)wv;
-                done[q] = true;
-              } else if (hi == tag_agg) {
-                c[q] += (unsigned)wv;
-                --jq[q];  // an aggregate: strip j's own total; keep looking left
-              }
-            }
-          }
-          bool all = true;
-#pragma unroll
-          for (int q = 0; q < SAT_RPT; ++q) all = all && done[q];
-          return __all_sync(FULL, all);
-        });
-        if (!ok) failed = true;
-      }
-#pragma unroll
-      for (int q = 0; q < SAT_RPT; ++q) {
-        if (live[q] && publish && !failed)
-          st_relaxed_gpu_u64(own + yq[q], ((unsigned long long)tag_inc << 32) | (c[q] + inc[q]));
-        const unsigned off = __shfl_sync(FULL, c[q], (lane & ~(SAT_SEG - 1)) | (SAT_SEG - 1)) + seg_excl[q];
-        int *rowp = tile + (rr + 32 * q) * SAT_PITCH + 33 * g;
-#pragma unroll
-        for (int i = 0; i < 32; ++i) rowp[i] = (int)(pv[q][i] + off);
-      }
-      // (2) D_y(x) in place.  The barrier also ORs every thread's own failure, so all
-      // warps take the same branch even when one gives up while another is between
-      // the barriers
-      if (__syncthreads_or(failed)) break;
-      // 3. column pass: t[y][x] = t[y-1][x] + D_y(x)
-      const int *cp = tile + sat_col(tid);
-      int *dst = P.table + y0 * ld + x;
-      const int rows = (int)(n2 - y0 + 1 < SAT_RB ? n2 - y0 + 1 : SAT_RB);
-      if (xok) {
-        if (rows == SAT_RB) {
-#pragma unroll 8
-          for (int r = 0; r < SAT_RB; ++r, dst += ld) {
-            col += (unsigned)cp[r * SAT_PITCH];
-            __stcs(dst, (int)col);
-          }
-        } else {
-          for (int r = 0; r < rows; ++r, dst += ld) {
-            col += (unsigned)cp[r * SAT_PITCH];
-            __stcs(dst, (int)col);
-          }
-        }
-      }
-    }
-    cp_async_wait<0>();  // nothing of this strip still in flight into shared memory
-  }
-}
 
 // ---------------------------------------------------------------------------
 // The tensor-map kernel (16-byte rows).
@@ -558,6 +405,210 @@ __global__ void __launch_bounds__(256) sat_tma_kernel(const __grid_constant__ CU
   if (tid == 128) bulk_wait_all();  // no store still reading shared memory at exit
 }
 
+// ---------------------------------------------------------------------------
+// Any row stride (the reference's n1 + 3 included): the same two roles over the
+// cp.async layout.  Column warps load their own columns of a block by 4-byte
+// cp.async (zero-filled past n1 and n2) and let an mbarrier count the copies
+// (cp.async.mbarrier.arrive); after a block's column pass, each thread reloads its
+// column of that stage with the block WS_STAGES further on.  Scan warps scan the
+// padded rows (a pad word per 32 columns: conflict-free) and look back as in the
+// tensor-map kernel.
+// ---------------------------------------------------------------------------
+#ifndef GME_SAT_WS_STAGES
+#define GME_SAT_WS_STAGES 6
+#endif
+constexpr int WS_STAGES = GME_SAT_WS_STAGES;
+constexpr size_t WS_SMEM = (size_t)WS_STAGES * SAT_RB * SAT_PITCH * sizeof(int);
+static_assert(SAT_W == 128 && SAT_RB == 32, "the two roles take 128 columns x 32 rows per block");
+
+__device__ __forceinline__ void cp_async_mbar_arrive(unsigned long long *bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(su32(bar)) : "memory");
+}
+
+__global__ void __launch_bounds__(256) sat_ws_kernel(SatParams P) {
+  extern __shared__ __align__(16) int ws_smem[];
+  __shared__ __align__(8) unsigned long long full[WS_STAGES], scanned[WS_STAGES];
+  __shared__ unsigned s_off[WS_STAGES][SAT_RB][SAT_SEG];
+  __shared__ int s_strip, s_abort;
+  __shared__ unsigned long long s_issued, s_consumed;  // blocks loaded / waited for (global count)
+  const int tid = threadIdx.x, lane = tid & 31;
+  const bool scan_role = tid < 128;
+  if (tid == 0) {
+    s_abort = 0;
+    s_issued = s_consumed = 0;
+    for (int i = 0; i < WS_STAGES; ++i) {
+      mbar_init(&full[i], 128);
+      mbar_init(&scanned[i], 128);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  Waiter W(P.timeout_ns, &P.ctrl[1], &s_abort);
+  const long long n1 = P.n1, n2 = P.n2, ld = P.ld;
+  const long long nblk = (n2 + SAT_RB - 1) / SAT_RB;
+  const int rr = (tid & 127) >> 2, g = tid & 3;  // scan role: row rr, segment g (4 lanes per row)
+  const int ct = tid & 127;                      // column role: the strip's column ct
+  unsigned long long kbase = 0;
+  bool failed = false;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_strip = s_abort ? P.strips : atomicAdd(&P.ctrl[0], 1);
+    __syncthreads();
+    const int s = s_strip;
+    if (s >= P.strips) break;
+    const long long x0 = (long long)s * SAT_W;  // the strip's columns are x0 + 1 .. x0 + W
+    unsigned long long *own = P.carry + (long long)s * P.cstride;
+    const unsigned long long *left = P.carry + (long long)(s > 0 ? s - 1 : 0) * P.cstride;
+    const bool publish = s + 1 < P.strips;
+    const unsigned tag_agg = P.tag, tag_inc = P.tag + 1u;
+    if (scan_role) {
+      unsigned p_inc = 0, p_excl = 0;
+      bool p_live = false;
+      long long p_y = 0;
+      for (long long b = 0; b <= nblk && !failed; ++b) {
+        const unsigned long long pre = (b >= 1 && s > 0 && p_live) ? ld_relaxed_gpu_u64(left + p_y) : 0ull;
+        unsigned c_inc = 0, c_excl = 0;
+        bool c_live = false;
+        long long c_y = 0;
+        if (b < nblk) {
+          const unsigned long long k = kbase + b;
+          const int st = (int)(k % WS_STAGES);
+          const unsigned par = (unsigned)((k / WS_STAGES) & 1ull);
+          if (!W.wait([&] { return __all_sync(FULL, mbar_test(&full[st], par)); })) {
+            failed = true;
+            break;
+          }
+          if (tid == 0) s_consumed = k + 1;
+          int *rowp = ws_smem + st * (SAT_RB * SAT_PITCH) + rr * SAT_PITCH + 33 * g;
+          unsigned pv[32];
+          unsigned acc = 0;
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            acc += (unsigned)rowp[i];  // zero past n1 (the copies zero-fill)
+            pv[i] = acc;
+          }
+#pragma unroll
+          for (int i = 0; i < 32; ++i) rowp[i] = (int)pv[i];
+          unsigned t = acc;
+#pragma unroll
+          for (int d = 1; d < SAT_SEG; d <<= 1) {
+            const unsigned u = __shfl_up_sync(FULL, t, d, SAT_SEG);
+            if (g >= d) t += u;
+          }
+          c_inc = t;
+          c_excl = t - acc;
+          c_y = 1 + b * SAT_RB + rr;
+          c_live = g == SAT_SEG - 1 && c_y <= n2;
+          if (s > 0 && c_live && publish) st_relaxed_gpu_u64(own + c_y, ((unsigned long long)tag_agg << 32) | c_inc);
+        }
+        if (b >= 1) {
+          unsigned c = 0;
+          bool done = !p_live;
+          long long jq = s - 1;
+          if (s == 0) {
+            if (p_live) c = (unsigned)P.table[p_y * ld] - (unsigned)P.table[(p_y - 1) * ld];
+          } else if (p_live) {
+            const unsigned hi = (unsigned)(pre >> 32);
+            if (hi == tag_inc) {
+              c = (unsigned)pre;
+              done = true;
+            } else if (hi == tag_agg) {
+              c = (unsigned)pre;
+              --jq;
+            }
+          }
+          if (s > 0 && !W.wait([&] {
+                if (!done) {
+                  const unsigned long long wv = ld_relaxed_gpu_u64(P.carry + jq * P.cstride + p_y);
+                  const unsigned hi = (unsigned)(wv >> 32);
+                  if (hi == tag_inc) {
+                    c += (unsigned)wv;
+                    done = true;
+                  } else if (hi == tag_agg) {
+                    c += (unsigned)wv;
+                    --jq;
+                  }
+                }
+                return __all_sync(FULL, done);
+              })) {
+            failed = true;
+            break;
+          }
+          if (p_live && publish) st_relaxed_gpu_u64(own + p_y, ((unsigned long long)tag_inc << 32) | (c + p_inc));
+          const int pst = (int)((kbase + b - 1) % WS_STAGES);
+          s_off[pst][rr][g] = __shfl_sync(FULL, c, (lane & ~(SAT_SEG - 1)) | (SAT_SEG - 1)) + p_excl;
+          mbar_arrive(&scanned[pst]);
+        }
+        p_inc = c_inc;
+        p_excl = c_excl;
+        p_live = c_live;
+        p_y = c_y;
+      }
+    } else {
+      const long long x = x0 + 1 + ct;
+      const bool xok = x <= n1;
+      unsigned col = xok ? (unsigned)P.table[x] : 0u;  // row 0
+      const int seg = ct >> 5;
+      auto issue = [&](long long b) {
+        const unsigned long long k = kbase + b;
+        const int st = (int)(k % WS_STAGES);
+        int *t = ws_smem + st * (SAT_RB * SAT_PITCH) + sat_col(ct);
+        const long long y0 = 1 + b * SAT_RB;
+        const int *src = P.table + y0 * ld + x;
+#pragma unroll 8
+        for (int r = 0; r < SAT_RB; ++r, src += ld) {
+          const bool ok = xok && y0 + r <= n2;
+          cp_async4(t + r * SAT_PITCH, ok ? src : P.table, ok);
+        }
+        cp_async_mbar_arrive(&full[st]);  // counts once this thread's copies have landed
+        if (ct == 0) s_issued = k + 1;
+      };
+      for (long long b = 0; b < WS_STAGES && b < nblk; ++b) issue(b);
+      for (long long b = 0; b < nblk; ++b) {
+        const unsigned long long k = kbase + b;
+        const int st = (int)(k % WS_STAGES);
+        if (!W.wait([&] { return __all_sync(FULL, mbar_test(&scanned[st], (unsigned)((k / WS_STAGES) & 1ull))); })) {
+          failed = true;
+          break;
+        }
+        const long long y0 = 1 + b * SAT_RB;
+        const int rows = (int)(n2 - y0 + 1 < SAT_RB ? n2 - y0 + 1 : SAT_RB);
+        const int *cp = ws_smem + st * (SAT_RB * SAT_PITCH) + sat_col(ct);
+        int *dst = P.table + y0 * ld + x;
+        if (xok) {
+          if (rows == SAT_RB) {
+#pragma unroll 8
+            for (int r = 0; r < SAT_RB; ++r, dst += ld) {
+              col += (unsigned)cp[r * SAT_PITCH] + s_off[st][r][seg];
+              __stcs(dst, (int)col);
+            }
+          } else {
+            for (int r = 0; r < rows; ++r, dst += ld) {
+              col += (unsigned)cp[r * SAT_PITCH] + s_off[st][r][seg];
+              __stcs(dst, (int)col);
+            }
+          }
+        }
+        if (b + WS_STAGES < nblk) issue(b + WS_STAGES);  // this thread's column of the stage is read
+      }
+      cp_async_wait<0>();  // no copy of this strip still landing
+    }
+    if (__syncthreads_or(failed)) {
+      // a wait gave up: every thread's copies land, and their arrivals on the stage
+      // barriers (bounded), before the CTA leaves
+      cp_async_wait<0>();
+      __syncthreads();
+      if (tid == 0)
+        for (unsigned long long k = s_consumed; k < s_issued; ++k)
+          for (int it = 0; it < (1 << 22) && !mbar_test(&full[k % WS_STAGES], (unsigned)((k / WS_STAGES) & 1ull)); ++it) {
+          }
+      __syncthreads();
+      break;
+    }
+    kbase += nblk;
+  }
+}
+
 using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -633,8 +684,9 @@ int sat_run(Workspace &ws, int *d_table, long long n1, long long n2, long long l
   static bool attr_set[64] = {};
   const bool known = ws.device >= 0 && ws.device < 64;
   if (!known || !attr_set[ws.device]) {
-    if ((e = cudaFuncSetAttribute(sat_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SAT_SMEM)) != cudaSuccess)
-      return ws.fail(e, "cudaFuncSetAttribute(sat_kernel)");
+    if ((e = cudaFuncSetAttribute(sat_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WS_SMEM)) !=
+        cudaSuccess)
+      return ws.fail(e, "cudaFuncSetAttribute(sat_ws_kernel)");
     if ((e = cudaFuncSetAttribute(sat_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TMA_SMEM)) !=
         cudaSuccess)
       return ws.fail(e, "cudaFuncSetAttribute(sat_tma_kernel)");
@@ -670,11 +722,11 @@ int sat_run(Workspace &ws, int *d_table, long long n1, long long n2, long long l
     P.tag = tag;
     P.ctrl = ws.ctrl;
     P.timeout_ns = timeout_ns;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sat_kernel, SAT_THREADS, SAT_SMEM);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sat_ws_kernel, 256, WS_SMEM);
     const int grid = (int)std::min<long long>(strips, (long long)ws.sms * std::max(occ, 1));
-    sat_kernel<<<grid, SAT_THREADS, SAT_SMEM, st>>>(P);
+    sat_ws_kernel<<<grid, 256, WS_SMEM, st>>>(P);
     ws.launches += 1;
-    if ((e = cudaGetLastError()) != cudaSuccess) return ws.fail(e, "sat_kernel");
+    if ((e = cudaGetLastError()) != cudaSuccess) return ws.fail(e, "sat_ws_kernel");
   }
   if (d_status) {
     sat_status_kernel<<<1, 1, 0, st>>>(ws.ctrl, d_status);
