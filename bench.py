@@ -870,9 +870,9 @@ def run_gme_sat(args):
         peak, basis = 6800.0, "fallback 6.8 TB/s"
     achieved = 8.0 * cells / t / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": profiled_traffic("sat_kernel_16384" if ld % 4 else "sat_tma_kernel_16384"),
+            "traffic": profiled_traffic("sat_ws_kernel_16384" if ld % 4 else "sat_tma_kernel_16384"),
             "peak_basis": basis, "bytes_per_cell": 8,
-            "kernel": ("sat_kernel" if ld % 4 else "sat_tma_kernel (tensor maps)") + " (one launch)"}
+            "kernel": ("sat_ws_kernel (cp.async)" if ld % 4 else "sat_tma_kernel (tensor maps)") + " (one launch)"}
     cpu = sat_cpu_baseline(host, n1, n2, ld) if rank == 0 and not args.no_cpu else None
     layout = "the reference's layout" if ld == n1 + 3 else "rows padded to 16 bytes"
     cfg = {"workload": f"summed-area table, {n1} x {n2} interior in {layout} "
