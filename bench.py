@@ -10,10 +10,13 @@ resident in HBM; `e2e` is the same metric through the C ABI with host buffers
 (host->device copies and the device->host result read inside the timed region).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gme|reference]
-                  [--workload ed65536|lcs8192|sw32768|lcs32768|batched]
+                  [--workload ed65536|lcs8192|sw32768|lcs32768|batched|served|path|sat|baselines]
 
 The batched workload is 16384 pairs, each length log-uniform in [64, 4096], kinds
-LCS/ED/SW one third each, all in one planned launch replayed as a CUDA graph.
+LCS/ED/SW one third each, all in one planned launch replayed as a CUDA graph.  The
+served workload submits a request stream to the server; sat is the reference's
+summed-area table; baselines times the plain path beside the reference's
+table-based strategies rebuilt on this GPU.
 """
 from __future__ import annotations
 
@@ -894,6 +897,76 @@ def run_gme_sat(args):
     return line
 
 
+def run_gme_baselines(args):
+    """The plain path beside the comparison baselines -- the reference's table-based
+    strategies on this GPU (the whole DP table in HBM; one launch per anti-diagonal of
+    128 x 64 tiles, LCS/GPU_TILE_SHARE.cu; or of cells, EditDistance/GPU.cu) -- on
+    the same edit-distance pairs, every result checked against the oracle."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    import __graft_entry__ as ge
+    ge.build()
+    import gpumemefficient_gb300 as g
+    from gpumemefficient_gb300 import synth
+    from oracle import oracle as O
+    ctx = g.Context(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    sp = stream.cuda_stream
+    sc = g.scoring()
+    out = torch.zeros(g.RESULT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    rows = []
+    l0 = ctx.launches
+    clocks = ClockSampler(local)
+    for n in args.baseline_sizes:
+        a, b = synth.ed_pair(n)
+        want = int(O.align(O.ED, a, b, threads=os.cpu_count() or 1)["score"])
+        da = torch.from_numpy(a).to(dev)
+        db = torch.from_numpy(b).to(dev)
+        table = torch.empty((n + 1) * (n + 1), dtype=torch.int32, device=dev)
+        runs = {
+            "plain (this library)": lambda: ctx.align_device(1, da.data_ptr(), n, db.data_ptr(), n, out.data_ptr(), stream=sp),
+            "tiles 128x64, a launch per tile anti-diagonal": lambda: ctx.baseline_align_device(
+                g.BASELINE_TILES, 1, da.data_ptr(), n, db.data_ptr(), n, table.data_ptr(), out.data_ptr(),
+                tile_x=64, tile_y=128, sc=sc, stream=sp),
+            "cells, a launch per cell anti-diagonal": lambda: ctx.baseline_align_device(
+                g.BASELINE_CELLS, 1, da.data_ptr(), n, db.data_ptr(), n, table.data_ptr(), out.data_ptr(), sc=sc,
+                stream=sp),
+        }
+        for name, fn in runs.items():
+            fn()
+            stream.synchronize()
+            got = int(np.frombuffer(out.cpu().numpy().tobytes(), g.RESULT_DTYPE)[0]["score"])
+            reps = 5 if name.startswith("plain") else 2
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+            stream.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            rows.append({"n": n, "strategy": name, "ms": ms, "gcups": n * n / ms / 1e6,
+                         "table_bytes": 0 if name.startswith("plain") else (n + 1) * (n + 1) * 4,
+                         "parity_vs_oracle": "ok" if got == want else "MISMATCH"})
+        del table
+    clk = clocks.stop()
+    plain = {r["n"]: r["gcups"] for r in rows if r["strategy"].startswith("plain")}
+    for r in rows:
+        r["plain_over_this"] = plain[r["n"]] / r["gcups"]
+    line = {"metric": METRIC, "value": plain[max(plain)], "unit": "GCUPS", "n_gpus": 1, "steps": 5, "warmup": 1,
+            "ms_per_step": min(r["ms"] for r in rows if r["n"] == max(plain) and r["strategy"].startswith("plain")),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "edit distance, one n x n pair per call (10% seeded edits): the plain path beside "
+                                   "the reference's table-based strategies rebuilt on this GPU",
+                       "rows": rows},
+            "clocks": clk, "gpu_launches": ctx.launches - l0, "roofline": None, "cpu_baseline": None}
+    ctx.close()
+    return line
+
+
 def _walk(ops):
     i = j = 0
     for c in ops:
@@ -931,6 +1004,8 @@ def main():
     p.add_argument("--rate-seconds", type=float, default=2.0, help="served workload: seconds per rate point")
     p.add_argument("--wave-cells", type=int, default=0, help="served workload: cells per launch at most (0 = default)")
     p.add_argument("--no-parity", action="store_true", help="skip the oracle parity check (tuning runs)")
+    p.add_argument("--baseline-sizes", type=int, nargs="+", default=[8192, 16384],
+                   help="baselines workload: square ED sizes")
     p.add_argument("--sat-layout", choices=["reference", "aligned"], default="reference",
                    help="sat workload: rows of n1 + 3 ints (the reference's), or rounded up to 16 bytes")
     p.add_argument("--sat-n", type=int, default=32768,
@@ -951,6 +1026,8 @@ def main():
         line = run_gme_path(args)
     elif args.workload == "sat":
         line = run_gme_sat(args)
+    elif args.workload == "baselines":
+        line = run_gme_baselines(args)
     else:
         line = run_gme(args)
         ws = dist_env()[0]

@@ -74,6 +74,7 @@ class ServerConfig(ctypes.Structure):
 
 
 SERVE_RING, SERVE_WAVES = 0, 1
+BASELINE_TILES, BASELINE_CELLS = 0, 1
 
 
 class ServerStats(ctypes.Structure):
@@ -137,6 +138,8 @@ def _declare(L):
     L.gme_align_path.argtypes = [_vp, c.c_int, _vp, c.c_int64, _vp, c.c_int64, c.POINTER(Scoring), _vp,
                                  c.c_int64, c.POINTER(c.c_int64), c.POINTER(c.c_int32)]
     L.gme_debug_wait_timeout.argtypes = [_vp, c.c_uint64, c.POINTER(c.c_int32)]
+    L.gme_baseline_align_device.argtypes = [_vp, c.c_int32, c.c_int32, _vp, c.c_int64, _vp, c.c_int64, _vp, _vp,
+                                            c.c_int32, c.c_int32, _vp, _vp]
     L.gme_launch_count.argtypes = [_vp]
     L.gme_launch_count.restype = c.c_int64
     for name in ("gme_ref_lcs", "gme_ref_ed", "gme_ref_sw"):
@@ -323,6 +326,16 @@ class Context:
         """``gme_sat_device``: in place on a device table, asynchronous on ``stream``."""
         _check(lib().gme_sat_device(self.handle, d_table, n1, n2, ld, d_status or None, stream or None),
                self.handle)
+
+    def baseline_align_device(self, strategy: int, kind: int, d_a: int, n1: int, d_b: int, n2: int, d_table: int,
+                              d_out: int, tile_x: int = 64, tile_y: int = 128, sc: Optional[Scoring] = None,
+                              stream: int = 0):
+        """A comparison baseline (not the product path): the whole table in d_table,
+        BASELINE_TILES (one launch per anti-diagonal of tiles) or BASELINE_CELLS (one
+        launch per anti-diagonal of cells); the result (gme_result) at d_out."""
+        sc = sc or scoring()
+        _check(lib().gme_baseline_align_device(self.handle, strategy, kind, d_a, n1, d_b, n2, ctypes.byref(sc),
+                                               d_table, tile_x, tile_y, d_out, stream), self.handle)
 
     def debug_wait_timeout(self, timeout_ns: int) -> int:
         """Runs a bounded device wait on a flag nothing sets; returns the kernel's status."""

@@ -739,6 +739,26 @@ gme_status gme_debug_wait_timeout(gme_context *ctx, uint64_t timeout_ns, int32_t
 
 int64_t gme_launch_count(const gme_context *ctx) { return ctx ? ctx->ws.launches : -1; }
 
+gme_status gme_baseline_align_device(gme_context *ctx, gme_baseline strategy, gme_kind kind, const int32_t *d_a,
+                                     int64_t n1, const int32_t *d_b, int64_t n2, const gme_scoring *sc,
+                                     int32_t *d_table, int32_t tile_x, int32_t tile_y, gme_result *d_out,
+                                     void *stream) {
+  if (!ctx || !d_a || !d_b || !d_table || !d_out || (strategy != GME_BASELINE_TILES && strategy != GME_BASELINE_CELLS))
+    return GME_ERR_INVALID;
+  gme_status s = check_sizes(ctx, kind, n1, n2, sc);
+  if (s != GME_OK) return s;
+  gme_scoring def = gme_default_scoring();
+  if (!sc) sc = &def;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  cudaStream_t prev = ctx->ws.sync_stream;
+  ctx->ws.sync_stream = st;
+  const int rc = gme::baseline_run(ctx->ws, (int)strategy, (int)kind, d_a, n1, d_b, n2, to_scoring(sc), d_table,
+                                   tile_x, tile_y, d_out, st);
+  ctx->ws.sync_stream = prev;
+  return to_status(rc);
+}
+
 }  // extern "C"
 
 namespace gme {

@@ -160,6 +160,9 @@ int serve_rows_mult(int NW, bool block);
 long long serve_team_bytes();
 cudaError_t serve_launch(const ServeArgs &a, cudaStream_t st);
 // summed-area table (gme_sat.cu)
+// comparison baselines (gme_baselines.cu): strategy 0 = tiles, 1 = cells
+int baseline_run(Workspace &ws, int strategy, int kind, const int *d_a, long long n1, const int *d_b, long long n2,
+                 const Scoring &sc, int *d_table, int TX, int TY, gme_result *d_out, cudaStream_t st);
 int sat_run(Workspace &ws, int *d_table, long long n1, long long n2, long long ld, int *d_status,
             cudaStream_t st, unsigned long long timeout_ns);
 long long sat_scratch_words(long long n1, long long n2);

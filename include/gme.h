@@ -335,6 +335,23 @@ gme_status gme_align_device_noalloc(gme_kind kind, const int32_t *d_a, int64_t n
  * kernel returned (expected GME_ERR_TIMEOUT after `timeout_ns`).  Tests use it to
  * show a wait that runs out ends with a status, not a hang. */
 gme_status gme_debug_wait_timeout(gme_context *ctx, uint64_t timeout_ns, int32_t *kernel_status);
+
+/* ---- Comparison baselines (not the product path) ----
+ * The reference's table-based strategies for the same recurrences, on this GPU, so
+ * that the plain path can be timed beside them.  d_table is the caller's
+ * (n2 + 1) x (n1 + 1) int32 table in device memory, written whole; d_out receives the
+ * bottom-right cell and, for SW, the first maximum in row-major order.  Needs
+ * 1 <= n1, n2 and (n1 + 1)(n2 + 1) < 2^32.
+ *   GME_BASELINE_TILES: tiles of tile_y x tile_x cells, one launch per anti-diagonal of
+ *     tiles, each swept in shared memory (LCS/GPU_TILE_SHARE.cu:12-207; the reference
+ *     uses 128 x 64);
+ *   GME_BASELINE_CELLS: one launch per anti-diagonal of cells, a thread per cell
+ *     (EditDistance/GPU.cu:20-60); tile_x and tile_y are not read. */
+typedef enum gme_baseline { GME_BASELINE_TILES = 0, GME_BASELINE_CELLS = 1 } gme_baseline;
+gme_status gme_baseline_align_device(gme_context *ctx, gme_baseline strategy, gme_kind kind, const int32_t *d_a,
+                                     int64_t n1, const int32_t *d_b, int64_t n2, const gme_scoring *sc,
+                                     int32_t *d_table, int32_t tile_x, int32_t tile_y, gme_result *d_out,
+                                     void *stream);
 /* Number of kernels this context launched since creation (the bench counts them). */
 int64_t gme_launch_count(const gme_context *ctx);
 
