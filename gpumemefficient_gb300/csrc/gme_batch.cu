@@ -441,6 +441,41 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
     else if (cells >= tune.block_min_cells && p.n2 > 32 * R * (NW - 1)) blockj.push_back((int)i);
     else warpj.push_back((int)i);
   }
+  // Team sizes: the tuned rule, or, for a batch whose CTA pairs leave CTAs of the grid
+  // idle (a few large pairs), teams sized by the pair's share of the grid: a pair of
+  // c cells takes min(groups, 8, ceil(c / (cells of the CTA pairs / CTAs for them)))
+  // CTAs.  Only for planned settings; a caller's own settings are kept as given.
+  std::vector<int> fill_T;  // per pair: team size of the fill rule (0: the tuned rule)
+  auto team_size = [&](int i) {
+    if (!fill_T.empty() && fill_T[i] > 0) return fill_T[i];
+    return std::max(2, std::min(8, (int)groups(pairs[i]) / std::max(1, tune.team_split)));
+  };
+  if (!tune.user_set && !blockj.empty()) {
+    long long units = 0;
+    for (int i : teamj) units += team_size(i);
+    const long long other = units + ((long long)warpj.size() + NW - 1) / NW;
+    const long long avail = grid0 - other;  // CTAs left for the CTA pairs
+    if (avail > (long long)blockj.size()) {
+      long long big = 0;
+      for (int i : blockj) big += (long long)pairs[i].n1 * pairs[i].n2;
+      const double per_cta = (double)big / (double)avail;
+      fill_T.assign((size_t)npairs, 0);
+      std::vector<int> keep;
+      for (int i : blockj) {
+        const gme_pair &p = pairs[i];
+        const long long G = groups(p);
+        const long long want = (long long)std::ceil((double)p.n1 * p.n2 / per_cta);
+        const int T = (int)std::min(std::min(G, 8ll), want);
+        if (T >= 2 && (long long)(p.n1 + 1) * (p.n2 + 1) < (1ll << 32)) {
+          fill_T[i] = T;
+          teamj.push_back(i);
+        } else {
+          keep.push_back(i);
+        }
+      }
+      blockj.swap(keep);
+    }
+  }
   // one kind after another (an SM then runs one kind's code at a time), longest first
   auto by_cells = [&](int x, int y) {
     if (pairs[x].kind != pairs[y].kind) return pairs[x].kind < pairs[y].kind;
@@ -487,12 +522,11 @@ int batch_plan(Workspace &ws, BatchArena &ar, const gme_pair *pairs, long long n
   size_t slot = 0;
   for (int i : blockj) add(i, 32 * R * NW, slot++);
   for (int i : warpj) add(i, 32 * R, slot++);
-  // a team of T = groups / team_split (2..8) CTAs per team job; members claimed in order
+  // a team of T CTAs per team job (team_size); members claimed in order
   ar.h_units.clear();
   for (size_t j = 0; j < teamj.size(); ++j) {
     add(teamj[j], 32 * R * NW, slot++);
-    const int G = (int)groups(pairs[teamj[j]]);
-    const int T = std::max(2, std::min(8, G / std::max(1, tune.team_split)));
+    const int T = team_size(teamj[j]);
     for (int t = 0; t < T; ++t) ar.h_units.push_back(make_int4((int)j, t, T, 0));
   }
   cudaError_t e;

@@ -283,6 +283,25 @@ def test_plan_graph_replay(gme_ctx):
         plan.close()
 
 
+def test_fill_teams(gme_ctx):
+    """A planned batch of a few large pairs, too few to fill the grid one pair per CTA:
+    the plan shares them among teams sized to the grid, and pairs with a single band
+    group stay on one CTA; results as the oracle's, SW positions included."""
+    import gpumemefficient_gb300 as g
+    rng = np.random.default_rng(515)
+    kinds = list(rng.integers(0, 3, 12)) + [0, 1, 2]
+    sa = [rng.integers(0, 4, int(k)) for k in rng.integers(2000, 4100, 12)] + \
+         [rng.integers(0, 4, 9000) for _ in range(3)]
+    sb = [rng.integers(0, 4, int(k)) for k in rng.integers(2000, 4100, 12)] + \
+         [rng.integers(0, 4, 1000) for _ in range(3)]
+    gme_ctx.set_batch_config()
+    for rule in (0, 1):
+        check_batch(gme_ctx, kinds, sa, sb, rule=rule)
+        st = gme_ctx.batch_stats()
+        assert st["team_jobs"] >= 10 and st["long_jobs"] == 0
+    check_batch(gme_ctx, kinds, sa, sb, sc=g.scoring(5, -4, -7))
+
+
 def test_rows_per_lane_config(gme_ctx):
     """2 rows per lane runs with 8 warps per CTA only: asked with 4 it is refused, and
     asked alone it takes 8; other values are refused."""
