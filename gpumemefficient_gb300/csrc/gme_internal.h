@@ -8,6 +8,10 @@
 
 #include "gme.h"
 
+#ifndef GME_PLAIN_CHUNK
+#define GME_PLAIN_CHUNK 32
+#endif
+
 namespace gme {
 
 struct Scoring;
@@ -110,6 +114,9 @@ struct BatchArena {
   int reserve_team(long long units, long long bytes, Workspace &ws);
   void release();
 };
+
+// columns per ring transaction (and per band-slot group) of the plain kernel
+constexpr int PLAIN_C = GME_PLAIN_CHUNK;
 
 // batched path (gme_batch.cu)
 bool batch_config_valid(int NW, int R = 4);

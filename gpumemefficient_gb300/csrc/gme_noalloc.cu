@@ -35,7 +35,7 @@ constexpr int kMaxGrid = 64;  // CTAs, hence band-boundary slots (grid + 2)
 constexpr int kMaxDevices = 64;
 constexpr long long kPadL = 261, kPadR = 352;  // the plain kernel's pads of the staged a[]
 constexpr long long kMaxBandRows = 1024;       // largest band the automatic shape picks
-constexpr long long kChunk = 16;               // columns per ring transaction
+constexpr long long kChunk = PLAIN_C;          // columns per ring transaction
 
 constexpr long long words(long long bytes) { return (bytes + 255) / 256 * 32; }  // 256-byte granules
 constexpr long long kCtrlWords = words(16 * sizeof(int));

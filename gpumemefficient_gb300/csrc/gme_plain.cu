@@ -192,8 +192,8 @@ int plain_run(Workspace &ws, int kind, const int *d_a, long long n1, const int *
   const long long nbands = (n2 + H - 1) / H;
   if (grid <= 0 || grid > nbands) grid = (int)std::min<long long>(nbands, ws.sms);
   const int nslot = grid + 2;
-  // the last warp writes C-column groups: a group starting at column <= n1 ends at < stride
-  const long long stride = ((n1 + 1 + C - 1) / C) * C + C;
+  // the I/O warp writes PLAIN_C-column groups: a group starting at column <= n1 ends at < stride
+  const long long stride = ((n1 + 1 + PLAIN_C - 1) / PLAIN_C) * PLAIN_C + PLAIN_C;
   // a_pad and its copy shifted by two, each a whole number of 16-byte groups
   const long long a_pad_len = (PADL + n1 + PADR + 3) / 4 * 4;
   const long long b_pad_len = nbands * H;

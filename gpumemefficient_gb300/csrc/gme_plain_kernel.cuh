@@ -75,12 +75,20 @@ struct PlainParams {
   unsigned long long timeout_ns;
 };
 
-template <int NW> struct __align__(16) PlainSmem {
+// Columns per ring transaction: a chunk of PC = pc_of<KIND> wavefront steps between
+// ring checks.  PLAIN_C (32) for LCS and ED; 16 for SW, whose per-row maxima leave
+// too few registers for 32-step chunks (GB300: SW 32768^2 in 3.84 ms at 16 against
+// 5.25 ms at 32; ED 65536^2 in 3.99 ms at 32 against 4.33 ms at 16).  The band slots'
+// stride is a multiple of PLAIN_C, hence of every kind's chunk.
+template <int KIND> constexpr int pc_of = (KIND == K_SW && PLAIN_C > 16) ? 16 : PLAIN_C;
+static_assert(PLAIN_C % 16 == 0 && RING % PLAIN_C == 0, "chunks of 16-byte groups that tile the ring");
+
+template <int NW, int PC> struct __align__(16) PlainSmem {
   int ring[NW + 1][RING];
-  int tag[NW + 1][RING / C];
+  int tag[NW + 1][RING / PC];
   int cons[NW + 1];
-  // where lanes other than 31 put their copy of an outgoing chunk (16-byte stores)
-  alignas(16) int sink[NW][C];
+  // where lanes other than 31 put their stores of the outgoing row (16-byte groups)
+  alignas(16) int sink[NW][PC];
   int band;
   int abort;
   SwBest best[NW + 1];
@@ -110,30 +118,66 @@ __device__ __forceinline__ void ld_syms16(const int *p, int *d) {
   }
 }
 
+// 16-byte store of the outgoing row: lane 31 writes into the ring, the other lanes
+// into the warp's sink.  No "memory" clobber, so that the compiler may place the
+// incoming-row loads across it; the chunk's release (which has one) orders these
+// stores before the tag.
+__device__ __forceinline__ void sts4(unsigned addr, int a, int b, int c, int d) {
+  asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d));
+}
+__device__ __forceinline__ void lds4(const int *p, int *d) {
+  const int4 q = *reinterpret_cast<const int4 *>(p);
+  d[0] = q.x; d[1] = q.y; d[2] = q.z; d[3] = q.w;
+}
+
 // ---------------------------------------------------------------------------
-// C wavefront steps of one lane (R rows), the plain kernel's form of the engine in
+// PC wavefront steps of one lane (R rows), the plain kernel's form of the engine in
 // gme_engine.cuh (same state, same order: the bottom row first and shuffled at once).
 // COST_TABLE: rt0/rt1 are the row's cost table, win holds selectors; COST_CMP: rt0 is
-// the row's symbol, win holds symbols.  The window refill (the next chunk's C
-// symbols at step R) uses 16-byte loads from sym_next.
+// the row's symbol, win holds symbols.  The window refill (the next chunk's PC
+// symbols at step R) uses 16-byte loads from sym_next; the incoming row's tag for
+// the next chunk is read one step later (tag_ahead -> tag_next).
+//
+// The incoming row (inc: this chunk's PC columns in the ring, already validated;
+// head: its first 4) is read in 16-byte groups four steps ahead of lane 31's
+// shuffles to lane 0, and the next chunk's first group is read into head at step
+// PC-4, after its tag (valid if that tag matches).  The outgoing row (lane 31's
+// bottom cell, one column per step) is stored in 16-byte groups every 4 steps at
+// out (OUT).  No lane holds a whole chunk of either row in registers.
 // ---------------------------------------------------------------------------
-template <int KIND, int R, int COST, int PAR, bool CHECKED, bool PADROWS>
+template <int KIND, int R, int COST, int PAR, bool CHECKED, bool PADROWS, bool OUT>
 __device__ __forceinline__ void plain_steps(const Rec<KIND> &rec, int (&cur)[R], int (&prv)[R], int &recv,
-                                            int &recv_prev, int (&win)[2 * C], const int *sym_next,
+                                            int &recv_prev, int (&win)[2 * pc_of<KIND>], const int *sym_next,
                                             const unsigned (&rt0)[R], const unsigned (&rt1)[R],
-                                            const int (&inv)[C], int (&outq)[C], int s0, int lane, int N,
-                                            unsigned padmask, int (&smax)[R], int (&sstep)[R]) {
-  static_assert(R < C, "the window refill at step R needs R < C");
+                                            const int *inc, int (&head)[4], const int *inc_next,
+                                            const int *tag_ahead, int &tag_next, unsigned out, int s0, int lane,
+                                            int N, unsigned padmask, int (&smax)[R], int (&sstep)[R]) {
+  constexpr int PC = pc_of<KIND>;
+  static_assert(R + 1 < PC - 4 && PC % 4 == 0, "the tag read precedes the next chunk's first group");
+  int iv[PC];  // the incoming row of this chunk (registers: only the groups in flight)
 #pragma unroll
-  for (int q = 0; q < C; ++q) {
-    if (q == R) ld_syms16<C>(sym_next, &win[(PAR ^ 1) * C]);
+  for (int k = 0; k < 4; ++k) iv[k] = head[k];
+  int oq[PC];  // the outgoing row of this chunk, stored every 4 steps
+#pragma unroll
+  for (int q = 0; q < PC; ++q) {
+    if (q % 4 == 0) {
+      if (q + 4 < PC) lds4(inc + q + 4, &iv[q + 4]);
+      else lds4(inc_next, head);
+    }
+    if (q == R) ld_syms16<PC>(sym_next, &win[(PAR ^ 1) * PC]);
+    if (q == R + 1) tag_next = ld_acquire_cta(tag_ahead);
     const int s = s0 + q;
     const int rcv = recv;
-    outq[q] = cur[R - 1];
+    oq[q] = cur[R - 1];  // lane 31: bottom cell after step s-1 (column s-32R)
+    if (OUT && q % 4 == 3) sts4(out + 4 * (q - 3), oq[q - 3], oq[q - 2], oq[q - 1], oq[q]);
+    // the incoming row at column s+1, which lane 31 passes to lane 0 for the next step;
+    // the chunk's last step sends nothing useful: lane 0 re-latches the next chunk's
+    // first column from the validated ring
+    const int nxt = (q + 1 < PC) ? iv[q + 1] : 0;
     int D[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const int sym = win[(PAR * C + q - r + 2 * C) % (2 * C)];
+      const int sym = win[(PAR * PC + q - r + 2 * PC) % (2 * PC)];
       const int c = (COST == COST_TABLE) ? prmt(rt0[r], rt1[r], sym)
                                          : (sym == (int)rt0[r] ? rec.ceq : rec.cne);
       D[r] = (r ? prv[r - 1] : recv_prev) + c;
@@ -156,10 +200,7 @@ __device__ __forceinline__ void plain_steps(const Rec<KIND> &rec, int (&cur)[R],
       }
       nv[r] = v;
       if (k == 0) {
-        // lane 31 feeds the incoming row to lane 0 through the same shuffle; the
-        // chunk's last step sends nothing useful: lane 0 re-latches the next
-        // chunk's first column from the validated ring values
-        const int send = (lane == 31) ? inv[q + 1 < C ? q + 1 : C - 1] : v;
+        const int send = (lane == 31) ? nxt : v;
         recv = __shfl_sync(FULL, send, (lane + 31) & 31);  // for step s+1
         recv_prev = rcv;
       }
@@ -173,17 +214,18 @@ __device__ __forceinline__ void plain_steps(const Rec<KIND> &rec, int (&cur)[R],
 // warp hands its bottom row to the next ring (the last active warp's ring is
 // drained to global memory by the band's I/O warp).
 //
-// The incoming row runs one chunk ahead: during chunk j the warp already reads
-// the tag and values of chunk j+1, so at the start of chunk j+1 the check is a
-// register compare.  In steady state this makes each warp trail the one above
-// by one extra chunk (C steps), which buys the latency of the shared loads.
+// The incoming row's tag runs one chunk ahead: during chunk j the warp already reads
+// the tag of chunk j+1, so at the start of chunk j+1 the check is a register
+// compare.  In steady state this makes each warp trail the one above by one extra
+// chunk (PC steps).  The values are read from the ring 16 bytes at a time, ahead of use.
 //
-// Chunk boundaries carry no divergent branch: every lane stores the outgoing chunk
-// (lane 31 into the ring, the others into a per-warp sink) and the release of its
-// tag and the consumption count are predicated stores of lane 31.
+// Chunk boundaries carry no divergent branch: every lane stores the outgoing row
+// every 4 steps (lane 31 into the ring, the others into a per-warp sink) and the
+// release of its tag and the consumption count are predicated stores of lane 31.
 template <int KIND, int R, int NW, int COST>
-__device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, int warp, int lane,
+__device__ void compute_band(const PlainParams &P, PlainSmem<NW, pc_of<KIND>> &S, int band, int warp, int lane,
                              Waiter &W, SwBest &tb) {
+  constexpr int PC = pc_of<KIND>;
   const Rec<KIND> rec(P.sc);
   const int N = P.N, M = P.M;
   const int yl = band * P.H + warp * 32 * R + lane * R + 1;  // first row of this lane
@@ -222,38 +264,28 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
   }
   const bool padwarp = __any_sync(FULL, padmask != 0);
 
-  // Symbol window for chunk 0: i in [0, C) at win[0..C), i in [-R, 0) at win[2C-R..2C).
-  // sym[i] is this lane's symbol index i (column i - r + 1 for row r); its base is
-  // 16-byte aligned: PADL - 1 is a multiple of 4, and lanes whose offset R*lane is 2
-  // mod 4 read the copy shifted by two.
+  // Symbol window for chunk 0: i in [0, PC) at win[0..PC), i in [-R, 0) at
+  // win[2PC-R..2PC).  sym[i] is this lane's symbol index i (column i - r + 1 for row
+  // r); its base is 16-byte aligned: PADL - 1 is a multiple of 4, and lanes whose
+  // offset R*lane is 2 mod 4 read the copy shifted by two.
   const int base = PADL - 1 - lane * R;
   const int *sym = ((base & 3) == 0) ? P.a_pad + base : P.a_pad2 + base + 2;
-  int win[2 * C];
-  ld_syms16<C>(sym, win);
-  ld_syms<R, R>(sym - R, &win[2 * C - R]);
+  int win[2 * PC];
+  ld_syms16<PC>(sym, win);
+  ld_syms<R, R>(sym - R, &win[2 * PC - R]);
 #pragma unroll
-  for (int k = C; k < 2 * C - R; ++k) win[k] = 0;
+  for (int k = PC; k < 2 * PC - R; ++k) win[k] = 0;
 
   const int *ring_in = S.ring[warp];
   int *ring_out = S.ring[warp + 1];
   int *tag_in = S.tag[warp], *tag_out = S.tag[warp + 1];
   int *cons_in = &S.cons[warp], *cons_out = &S.cons[warp + 1];
-  int *const sinkp = S.sink[warp];
+  const unsigned sink = smem_addr(S.sink[warp]);
   int cons_seen = 0;
   int recv = 0, recv_prev = 0;
-
-  // incoming-row buffers by chunk parity: ib[PAR] holds chunk j, ib[PAR^1] chunk j+1
-  int ib[2][C];
-  int tag_next;
-  auto load_in = [&](int j, int (&dst)[C]) {
-#pragma unroll
-    for (int k = 0; k < C; k += 4) {
-      const int4 q = *reinterpret_cast<const int4 *>(&ring_in[(C * j + k) & (RING - 1)]);
-      dst[k] = q.x; dst[k + 1] = q.y; dst[k + 2] = q.z; dst[k + 3] = q.w;
-    }
-  };
-  tag_next = ld_acquire_cta(&tag_in[0]);
-  load_in(0, ib[0]);
+  int tag_next = ld_acquire_cta(&tag_in[0]);
+  int head[4];  // the incoming row's first 4 columns of the next chunk
+  lds4(ring_in, head);
 
   // OUT: 1 = the chunk's outgoing columns start at or after 0, 0 = before (no output),
   // 2 = decided per chunk (pad warps)
@@ -261,41 +293,35 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
     constexpr int PAR = decltype(par)::value;
     constexpr bool CK = decltype(checked)::value, PD = decltype(padrows)::value;
     constexpr int OUT = decltype(out)::value;
-    int(&inv)[C] = ib[PAR];
-    const int s0 = C * j;
+    const int s0 = PC * j;
     if (s0 <= N && !__all_sync(FULL, tag_next == j + 1)) {
-      // the read-ahead found the chunk not yet written: wait for it, then reread.
-      // Lanes may read the tag at different moments; the decision is warp-uniform
-      // so that no lane leaves the wait alone.
-      auto ready = [&] { return __all_sync(FULL, ld_acquire_cta(&tag_in[j & (RING / C - 1)]) == j + 1); };
+      // the read-ahead found the chunk not yet written: wait for it.  Lanes may read
+      // the tag at different moments; the decision is warp-uniform so that no lane
+      // leaves the wait alone.
+      auto ready = [&] { return __all_sync(FULL, ld_acquire_cta(&tag_in[j & (RING / PC - 1)]) == j + 1); };
       if (!W.wait(ready)) return false;
-      load_in(j, inv);
+      lds4(&ring_in[s0 & (RING - 1)], head);
     }
-    sts_vol_if(lane == 31, cons_in, s0 + C);
-    if (lane == 0) recv = inv[0];  // the incoming row's column s0 (see plain_steps)
-    // read ahead: chunk j+1
-    tag_next = ld_acquire_cta(&tag_in[(j + 1) & (RING / C - 1)]);
-    load_in(j + 1, ib[PAR ^ 1]);
-
-    int outq[C];
-    plain_steps<KIND, R, COST, PAR, CK, PD>(rec, cur, prv, recv, recv_prev, win, sym + s0 + C, rt0, rt1,
-                                            inv, outq, s0, lane, N, padmask, smax, sstep);
-    // outgoing row: columns pos..pos+C-1, pos = s0 - 32R (chunk j - 2R)
+    // columns before s0 are consumed: their slots may be refilled
+    sts_vol_if(lane == 31, cons_in, s0);
+    const int *inc = &ring_in[s0 & (RING - 1)];
+    if (lane == 0) recv = head[0];  // the incoming row's column s0 (see plain_steps)
+    // outgoing row: columns pos..pos+PC-1, pos = s0 - 32R, stored 4 columns at a time
     const int pos = s0 - 32 * R;
-    if (OUT == 1 || (OUT == 2 && pos >= 0)) {
-      if (pos + C - RING > cons_seen) {
-        if (!W.wait([&] {
-              cons_seen = __shfl_sync(FULL, lds_vol(cons_out), 0);
-              return cons_seen >= pos + C - RING;
-            }))
-          return false;
-      }
-      int *dst = (lane == 31) ? &ring_out[pos & (RING - 1)] : sinkp;
-#pragma unroll
-      for (int k = 0; k < C; k += 4)
-        *reinterpret_cast<int4 *>(dst + k) = make_int4(outq[k], outq[k + 1], outq[k + 2], outq[k + 3]);
-      st_release_cta_if(lane == 31, &tag_out[(pos / C) & (RING / C - 1)], pos / C + 1);
+    const bool out_on = OUT == 1 || (OUT == 2 && pos >= 0);
+    if (OUT != 0 && out_on && pos + PC - RING > cons_seen) {
+      if (!W.wait([&] {
+            cons_seen = __shfl_sync(FULL, lds_vol(cons_out), 0);
+            return cons_seen >= pos + PC - RING;
+          }))
+        return false;
     }
+    const unsigned outp = (lane == 31 && out_on) ? smem_addr(&ring_out[pos & (RING - 1)]) : sink;
+    plain_steps<KIND, R, COST, PAR, CK, PD, OUT != 0>(rec, cur, prv, recv, recv_prev, win, sym + s0 + PC, rt0,
+                                                      rt1, inc, head, &ring_in[(s0 + PC) & (RING - 1)],
+                                                      &tag_in[(j + 1) & (RING / PC - 1)], tag_next, outp, s0,
+                                                      lane, N, padmask, smax, sstep);
+    if (out_on) st_release_cta_if(lane == 31, &tag_out[(pos / PC) & (RING / PC - 1)], pos / PC + 1);
     return true;
   };
 
@@ -321,11 +347,11 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
   using O1 = std::integral_constant<int, 1>;
   using O2 = std::integral_constant<int, 2>;
   // last chunk: its output covers column N (outputs lag the inputs by 32R columns)
-  const int j_end = (N + 32 * R) / C;
+  const int j_end = (N + 32 * R) / PC;
   // chunks 0 .. j_out-1 produce no output (their columns are left of column 0)
-  const int j_out = min((32 * R) / C, j_end + 1);
-  // chunks 0 .. j_full have every cell of the warp at x <= N (none when N < C - 1)
-  const int j_full = (N >= C - 1) ? min((N - C + 1) / C, j_end) : -1;
+  const int j_out = min((32 * R) / PC, j_end + 1);
+  // chunks 0 .. j_full have every cell of the warp at x <= N (none when N < PC - 1)
+  const int j_full = (N >= PC - 1) ? min((N - PC + 1) / PC, j_end) : -1;
   if (padwarp) {
     if (!range(0, j_end, T{}, T{}, O2{})) return;
   } else {
@@ -335,7 +361,7 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
     const int j_in = (COST == COST_TABLE) ? min(j_out - 1, j_full) : -1;
     if (!range(0, j_in, F{}, F{}, O0{})) return;
     if (!range(j_in + 1, j_out - 1, T{}, F{}, O0{})) return;
-    // steady chunks: every cell of the warp has 1 <= x <= N for all C steps
+    // steady chunks: every cell of the warp has 1 <= x <= N for all PC steps
     const int j_hi = max(j_full, j_out - 1);
     if (!range(j_out, j_hi, F{}, F{}, O1{})) return;
     // ramp-out: cells beyond column N hold their value at column N
@@ -363,7 +389,8 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW> &S, int band, i
 // global poll is issued first and consumed last, so its L2 round trip overlaps
 // the drain.
 template <int KIND, int NW>
-__device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int active, int lane) {
+__device__ void io_band(const PlainParams &P, PlainSmem<NW, pc_of<KIND>> &S, int band, int active, int lane) {
+  constexpr int PC = pc_of<KIND>;
   const int N1 = P.N + 1;
   const unsigned long long *src =
       band > 0 ? P.slots + (long long)((band - 1) % P.nslot) * P.slot_stride : nullptr;
@@ -389,26 +416,26 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int ac
       asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2];" : "=l"(w[0]), "=l"(w[1]) : "l"(sp));
       asm volatile("ld.volatile.global.v2.u64 {%0,%1}, [%2+16];" : "=l"(w[2]), "=l"(w[3]) : "l"(sp));
     }
-    // (b) outgoing: lane k looks at chunk out_pos/C + k
+    // (b) outgoing: lane k looks at chunk out_pos/PC + k
     if (out_pos < N1) {
-      const int c = out_pos / C + lane;
+      const int c = out_pos / PC + lane;
       bool ready = false;
-      if (lane < 8 && c * C < N1) ready = ld_acquire_cta(&tago[c & (RING / C - 1)]) == c + 1;
+      if (lane < 8 && c * PC < N1) ready = ld_acquire_cta(&tago[c & (RING / PC - 1)]) == c + 1;
       const unsigned rm = __ballot_sync(FULL, ready);
       const int nch = (rm == FULL) ? 32 : (__ffs(~rm) - 1);
       if (nch > 0) {
         if (lane < nch) {
 #pragma unroll
-          for (int k = 0; k < C; k += 4) {
-            const int4 q = *reinterpret_cast<const int4 *>(&ringo[(c * C + k) & (RING - 1)]);
-            volatile unsigned long long *dp = dst + c * C + k;
+          for (int k = 0; k < PC; k += 4) {
+            const int4 q = *reinterpret_cast<const int4 *>(&ringo[(c * PC + k) & (RING - 1)]);
+            volatile unsigned long long *dp = dst + c * PC + k;
             const unsigned long long w0 = dst_tag | (unsigned)q.x, w1 = dst_tag | (unsigned)q.y;
             const unsigned long long w2 = dst_tag | (unsigned)q.z, w3 = dst_tag | (unsigned)q.w;
             asm volatile("st.volatile.global.v2.u64 [%0], {%1,%2};" :: "l"(dp), "l"(w0), "l"(w1) : "memory");
             asm volatile("st.volatile.global.v2.u64 [%0+16], {%1,%2};" :: "l"(dp), "l"(w2), "l"(w3) : "memory");
           }
         }
-        out_pos = min(out_pos + nch * C, N1);
+        out_pos = min(out_pos + nch * PC, N1);
         __syncwarp();
         if (lane == 0) sts_vol(&S.cons[active], out_pos);
         moved = true;
@@ -436,9 +463,9 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int ac
           *reinterpret_cast<int4 *>(&ring0[p & (RING - 1)]) = make_int4(v[0], v[1], v[2], v[3]);
         __syncwarp();
         // release the chunks this round completed (the last one may be partial)
-        const int c0 = in_pos / C;
-        const int c1 = (in_pos + n >= N1) ? (N1 + C - 1) / C : (in_pos + n) / C;
-        if (lane < c1 - c0) st_release_cta(&S.tag[0][(c0 + lane) & (RING / C - 1)], c0 + lane + 1);
+        const int c0 = in_pos / PC;
+        const int c1 = (in_pos + n >= N1) ? (N1 + PC - 1) / PC : (in_pos + n) / PC;
+        if (lane < c1 - c0) st_release_cta(&S.tag[0][(c0 + lane) & (RING / PC - 1)], c0 + lane + 1);
         in_pos += n;
         moved = true;
       }
@@ -467,7 +494,8 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW> &S, int band, int ac
 
 template <int KIND, int R, int NW>
 __global__ void __launch_bounds__((NW + 1) * 32, 1) plain_kernel(PlainParams P) {
-  __shared__ PlainSmem<NW> S;
+  constexpr int PC = pc_of<KIND>;
+  __shared__ PlainSmem<NW, PC> S;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) S.abort = 0;
   __syncthreads();
@@ -480,7 +508,7 @@ __global__ void __launch_bounds__((NW + 1) * 32, 1) plain_kernel(PlainParams P) 
 #pragma unroll
       for (int k = 0; k <= NW; ++k) S.cons[k] = 0;
     }
-    for (int i = threadIdx.x; i < (NW + 1) * (RING / C); i += blockDim.x) (&S.tag[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < (NW + 1) * (RING / PC); i += blockDim.x) (&S.tag[0][0])[i] = 0;
     __syncthreads();
     const int band = S.band;
     if (band >= P.nbands) break;

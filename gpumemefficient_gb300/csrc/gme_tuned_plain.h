@@ -12,12 +12,12 @@ struct TunedPlain {
 
 constexpr int TUNED_PLAIN = 6;
 constexpr TunedPlain TUNED_PLAIN_TABLE[TUNED_PLAIN > 0 ? TUNED_PLAIN : 1] = {
-    {2048, 4, 4},  // 29 GCUPS
-    {4096, 4, 4},  // 62 GCUPS
-    {8192, 4, 4},  // 127 GCUPS
-    {16384, 4, 4},  // 259 GCUPS
-    {32768, 4, 4},  // 518 GCUPS
-    {65536, 4, 4},  // 1042 GCUPS
+    {2048, 2, 4},  // 32 GCUPS
+    {4096, 2, 4},  // 67 GCUPS
+    {8192, 2, 4},  // 139 GCUPS
+    {16384, 2, 4},  // 283 GCUPS
+    {32768, 2, 4},  // 570 GCUPS
+    {65536, 2, 4},  // 1154 GCUPS
 };
 
 }  // namespace gme
