@@ -80,7 +80,10 @@ struct PlainParams {
 // too few registers for 32-step chunks (GB300: SW 32768^2 in 3.84 ms at 16 against
 // 5.25 ms at 32; ED 65536^2 in 3.99 ms at 32 against 4.33 ms at 16).  The band slots'
 // stride is a multiple of PLAIN_C, hence of every kind's chunk.
-template <int KIND> constexpr int pc_of = (KIND == K_SW && PLAIN_C > 16) ? 16 : PLAIN_C;
+#ifndef GME_PLAIN_CHUNK_SW
+#define GME_PLAIN_CHUNK_SW 16
+#endif
+template <int KIND> constexpr int pc_of = (KIND == K_SW && PLAIN_C > GME_PLAIN_CHUNK_SW) ? GME_PLAIN_CHUNK_SW : PLAIN_C;
 static_assert(PLAIN_C % 16 == 0 && RING % PLAIN_C == 0, "chunks of 16-byte groups that tile the ring");
 
 template <int NW, int PC> struct __align__(16) PlainSmem {
