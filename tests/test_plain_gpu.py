@@ -60,6 +60,28 @@ def test_random_shapes(gme_ctx, kind, cfg):
         gme_ctx.set_plain_config(0, 0, 0)
 
 
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_chunk_boundaries(gme_ctx, cfg):
+    """Widths around the chunk length (16 and 32 columns), the 32R-column skew of a
+    warp's output (64, 128) and their sums, against heights around the band heights
+    (256, 512, 1024 rows); all kinds, table and compare forms."""
+    rng = np.random.default_rng(900 + cfg[0] * 10 + cfg[1])
+    widths = [1, 2, 3, 4, 5, 15, 16, 17, 31, 32, 33, 63, 64, 65, 95, 96, 97, 127, 128, 129, 159, 160, 161,
+              191, 192, 193, 255, 256, 257]
+    heights = [1, 63, 255, 257, 511, 1025]
+    gme_ctx.set_plain_config(*cfg)
+    try:
+        for i, n1 in enumerate(widths):
+            for j, n2 in enumerate(heights):
+                alpha = 4 if (i + j) % 2 == 0 else 20
+                a = rng.integers(0, alpha, n1)
+                b = rng.integers(0, alpha, n2)
+                for kind in (0, 1, 2):
+                    check(gme_ctx, kind, a, b, rule=(i + j + kind) % 2)
+    finally:
+        gme_ctx.set_plain_config(0, 0, 0)
+
+
 @pytest.mark.parametrize("kind", [0, 1, 2])
 def test_extremes(gme_ctx, kind):
     rng = np.random.default_rng(7)
