@@ -84,6 +84,14 @@ struct PlainParams {
 #define GME_PLAIN_CHUNK_SW 16
 #endif
 template <int KIND> constexpr int pc_of = (KIND == K_SW && PLAIN_C > GME_PLAIN_CHUNK_SW) ? GME_PLAIN_CHUNK_SW : PLAIN_C;
+
+// I/O warps per CTA: 2 = one for the incoming row (global slot -> ring 0), one for
+// the outgoing row (last ring -> global slot); 1 = one warp doing both in turn.
+#ifndef GME_PLAIN_IO_WARPS
+#define GME_PLAIN_IO_WARPS 2
+#endif
+constexpr int PLAIN_IO = GME_PLAIN_IO_WARPS;
+static_assert(PLAIN_IO == 1 || PLAIN_IO == 2, "one or two I/O warps");
 static_assert(PLAIN_C % 16 == 0 && RING % PLAIN_C == 0, "chunks of 16-byte groups that tile the ring");
 
 template <int NW, int PC> struct __align__(16) PlainSmem {
@@ -94,7 +102,7 @@ template <int NW, int PC> struct __align__(16) PlainSmem {
   alignas(16) int sink[NW][PC];
   int band;
   int abort;
-  SwBest best[NW + 1];
+  SwBest best[NW + PLAIN_IO];
 };
 
 __device__ __forceinline__ void st_release_cta_if(bool p, int *a, int v) {
@@ -385,14 +393,17 @@ __device__ void compute_band(const PlainParams &P, PlainSmem<NW, pc_of<KIND>> &S
   }
 }
 
-// The I/O warp of a band.  Incoming row: forwards the band above's tagged global
+// The I/O warps of a band.  Incoming row: forwards the band above's tagged global
 // words (or, for band 0, the table's top border) into ring 0 and releases each
 // completed chunk.  Outgoing row: copies the chunks the last compute warp has
-// released from ring `active` to the band's global slot as tagged words.  The
-// global poll is issued first and consumed last, so its L2 round trip overlaps
-// the drain.
+// released from ring `active` to the band's global slot as tagged words.  Role 0
+// does both in one loop (the global poll issued first and consumed last, so its L2
+// round trip overlaps the drain); role 1 only the incoming row, role 2 only the
+// outgoing one, so that a released chunk leaves within a shared-memory poll rather
+// than within a global one.
 template <int KIND, int NW>
-__device__ void io_band(const PlainParams &P, PlainSmem<NW, pc_of<KIND>> &S, int band, int active, int lane) {
+__device__ void io_band(const PlainParams &P, PlainSmem<NW, pc_of<KIND>> &S, int band, int active, int lane,
+                        int role) {
   constexpr int PC = pc_of<KIND>;
   const int N1 = P.N + 1;
   const unsigned long long *src =
@@ -403,7 +414,7 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW, pc_of<KIND>> &S, int
   int *ring0 = S.ring[0];
   const int *ringo = S.ring[active];
   const int *tago = S.tag[active];
-  int in_pos = 0, out_pos = 0;
+  int in_pos = role == 2 ? N1 : 0, out_pos = role == 1 ? N1 : 0;
   unsigned idle = 0;
   unsigned long long deadline = 0;
 
@@ -490,13 +501,14 @@ __device__ void io_band(const PlainParams &P, PlainSmem<NW, pc_of<KIND>> &S, int
           return;
         }
       }
-      if (band == 0 || in_pos >= N1) __nanosleep(128);
+      if (role == 2) __nanosleep(32);
+      else if (band == 0 || in_pos >= N1) __nanosleep(128);
     }
   }
 }
 
 template <int KIND, int R, int NW>
-__global__ void __launch_bounds__((NW + 1) * 32, 1) plain_kernel(PlainParams P) {
+__global__ void __launch_bounds__((NW + PLAIN_IO) * 32, 1) plain_kernel(PlainParams P) {
   constexpr int PC = pc_of<KIND>;
   __shared__ PlainSmem<NW, PC> S;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -523,7 +535,7 @@ __global__ void __launch_bounds__((NW + 1) * 32, 1) plain_kernel(PlainParams P) 
         else compute_band<KIND, R, NW, COST_CMP>(P, S, band, warp, lane, W, tb);
       }
     } else {
-      io_band<KIND, NW>(P, S, band, active, lane);
+      io_band<KIND, NW>(P, S, band, active, lane, PLAIN_IO == 1 ? 0 : warp - NW + 1);
     }
     __syncthreads();
   }
@@ -542,7 +554,7 @@ __global__ void __launch_bounds__((NW + 1) * 32, 1) plain_kernel(PlainParams P) 
     __syncthreads();
     if (threadIdx.x == 0) {
       SwBest b = S.best[0];
-      for (int k = 1; k <= NW; ++k)
+      for (int k = 1; k < NW + PLAIN_IO; ++k)
         if (better(S.best[k], b)) b = S.best[k];
       P.best[blockIdx.x] = b;
     }
@@ -551,7 +563,7 @@ __global__ void __launch_bounds__((NW + 1) * 32, 1) plain_kernel(PlainParams P) 
 
 template <int KIND, int R, int NW>
 inline cudaError_t launch_plain_t(const PlainParams &P, int grid, cudaStream_t st) {
-  plain_kernel<KIND, R, NW><<<grid, (NW + 1) * 32, 0, st>>>(P);
+  plain_kernel<KIND, R, NW><<<grid, (NW + PLAIN_IO) * 32, 0, st>>>(P);
   return cudaGetLastError();
 }
 
