@@ -77,9 +77,10 @@ struct PlainParams {
 
 // Columns per ring transaction: a chunk of PC = pc_of<KIND> wavefront steps between
 // ring checks.  PLAIN_C (32) for LCS and ED; 16 for SW, whose per-row maxima leave
-// too few registers for 32-step chunks (GB300: SW 32768^2 in 3.84 ms at 16 against
-// 5.25 ms at 32; ED 65536^2 in 3.99 ms at 32 against 4.33 ms at 16).  The band slots'
-// stride is a multiple of PLAIN_C, hence of every kind's chunk.
+// too few registers for 32-step chunks.  Measured on GB300 at 4 rows per lane: SW
+// 32768^2 3.84 ms at 16 against 5.25 ms at 32, ED 65536^2 3.99 ms at 32 against
+// 4.33 ms at 16; at 2 rows per lane: SW 2.77 against 2.89 ms, ED 3.74 against 4.24 ms.
+// The band slots' stride is a multiple of PLAIN_C, hence of every kind's chunk.
 #ifndef GME_PLAIN_CHUNK_SW
 #define GME_PLAIN_CHUNK_SW 16
 #endif
